@@ -1,0 +1,274 @@
+"""heterosync_gb300 -- GB300-native (sm_103a) HeteroSync hot path.
+
+Python mirror of the C ABI in include/hs/hs.h (libhsgb300.so, loaded with
+ctypes).  The names follow the reference (heterosync cuda/syncPrims/uvm/main.cu):
+primitives are addressed by the same strings as the ``allSyncPrims-1kernel``
+command line ("faMutex", "spinSemEBO10", "lfTreeBarrUniqLocalExch", ...), and a
+run takes the same four numbers (numLdSt, numTBs, numCSIters plus the threads
+per TB the reference fixes at compile time).
+
+There is no CPU fallback: if the CUDA library has not been built, importing
+works (so the host-side helpers stay usable) but every call that needs the
+library raises ``HsLibraryMissing``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass, field
+from typing import Optional
+
+__all__ = [
+    "HsError", "HsLibraryMissing", "RunConfig", "RunResult", "PRIM_NAMES", "prim_id", "prim_name",
+    "prim_label", "storage_words", "expected_storage", "run", "lib", "lib_path", "launch_count",
+    "device_info", "MODE_REF", "MODE_INC", "MODE_SLICE",
+]
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_PKG, "lib", "libhsgb300.so")
+
+MODE_REF, MODE_INC, MODE_SLICE = 0, 1, 2
+_MODES = {"ref": MODE_REF, "inc": MODE_INC, "slice": MODE_SLICE}
+
+HS_OK, HS_EINVAL, HS_ETIMEDOUT, HS_ENORES, HS_ECUDA, HS_ENODEV, HS_EMISMATCH = range(7)
+RUN_SYNC_EACH, RUN_KEEP_STATE = 1, 2
+
+# Reference names and ids, main.cu:1224-1256.
+PRIM_NAMES = {
+    "atomicTreeBarrUniq": 0, "atomicTreeBarrUniqLocalExch": 1, "lfTreeBarrUniq": 2,
+    "lfTreeBarrUniqLocalExch": 3, "spinMutex": 4, "spinMutexEBO": 5, "sleepMutex": 6, "faMutex": 7,
+    "spinSem1": 8, "spinSem2": 9, "spinSem10": 10, "spinSem120": 11, "spinSemEBO1": 12,
+    "spinSemEBO2": 13, "spinSemEBO10": 14, "spinSemEBO120": 15, "spinMutexUniq": 20,
+    "spinMutexEBOUniq": 21, "sleepMutexUniq": 22, "faMutexUniq": 23, "spinSemUniq1": 24,
+    "spinSemUniq2": 25, "spinSemUniq10": 26, "spinSemUniq120": 27, "spinSemEBOUniq1": 28,
+    "spinSemEBOUniq2": 29, "spinSemEBOUniq10": 30, "spinSemEBOUniq120": 31,
+}
+_ID_TO_NAME = {v: k for k, v in PRIM_NAMES.items()}
+
+
+class HsError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__("%s (status %d)" % (msg, status))
+        self.status = status
+
+
+class HsLibraryMissing(HsError):
+    pass
+
+
+class _RunConfig(ctypes.Structure):
+    _fields_ = [
+        ("prim", ctypes.c_int), ("num_ldst", ctypes.c_int), ("num_tbs", ctypes.c_int),
+        ("num_iters", ctypes.c_int), ("threads", ctypes.c_int), ("repeats", ctypes.c_int),
+        ("mode", ctypes.c_int), ("nsm", ctypes.c_int), ("backoff_min_ns", ctypes.c_uint),
+        ("backoff_max_ns", ctypes.c_uint), ("backoff_unit_ns", ctypes.c_uint),
+        ("timeout_ns", ctypes.c_ulonglong), ("skip_tb", ctypes.c_int), ("flags", ctypes.c_int),
+    ]
+
+
+class _RunResult(ctypes.Structure):
+    _fields_ = [
+        ("status", ctypes.c_int), ("dev_error_bits", ctypes.c_uint), ("dev_error_site", ctypes.c_uint),
+        ("elapsed_ms", ctypes.c_float), ("avg_ms", ctypes.c_float), ("h2d_ms", ctypes.c_float),
+        ("d2h_ms", ctypes.c_float), ("ops", ctypes.c_ulonglong), ("launches", ctypes.c_uint),
+    ]
+
+
+_lib = None
+_ctx = None
+
+
+def lib_path() -> str:
+    return _LIB_PATH
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded libhsgb300.so (raises HsLibraryMissing if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            raise HsLibraryMissing(HS_ENODEV, "libhsgb300.so not built: run `python -m heterosync_gb300.build` "
+                                   "(expected at %s)" % _LIB_PATH)
+        L = ctypes.CDLL(_LIB_PATH)
+        L.hs_last_error.restype = ctypes.c_char_p
+        L.hs_status_string.restype = ctypes.c_char_p
+        L.hs_prim_name.restype = ctypes.c_char_p
+        L.hs_launch_count.restype = ctypes.c_ulonglong
+        L.hs_prim_id.argtypes = [ctypes.c_char_p]
+        L.hs_storage_words.argtypes = [ctypes.POINTER(_RunConfig), ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]
+        L.hs_run.argtypes = [ctypes.c_void_p, ctypes.POINTER(_RunConfig), ctypes.c_void_p, ctypes.c_int,
+                             ctypes.c_void_p, ctypes.POINTER(_RunResult)]
+        L.hs_expected_storage.argtypes = [ctypes.POINTER(_RunConfig), ctypes.c_int, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_size_t]
+        L.hs_ctx_create.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+        L.hs_ctx_destroy.argtypes = [ctypes.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _err(status: int) -> HsError:
+    L = lib()
+    return HsError(status, "%s: %s" % (L.hs_status_string(status).decode(), L.hs_last_error().decode()))
+
+
+def launch_count() -> int:
+    """Kernels launched by the library in this process."""
+    return int(lib().hs_launch_count())
+
+
+def device_info(device: int = 0) -> dict:
+    vals = [ctypes.c_int() for _ in range(4)]
+    s = lib().hs_device_info(device, *[ctypes.byref(v) for v in vals])
+    if s:
+        raise _err(s)
+    return {"nsm": vals[0].value, "cc": (vals[1].value, vals[2].value), "max_threads_per_block": vals[3].value}
+
+
+def prim_id(name) -> int:
+    if isinstance(name, int):
+        if name not in _ID_TO_NAME:
+            raise ValueError("unknown syncPrim id %d" % name)
+        return name
+    if name not in PRIM_NAMES:
+        raise ValueError("ERROR: Unknown synchronization primitive: %s" % name)
+    return PRIM_NAMES[name]
+
+
+def prim_name(pid: int) -> str:
+    return _ID_TO_NAME[pid]
+
+
+def prim_label(prim, num_iters: int) -> str:
+    buf = ctypes.create_string_buffer(128)
+    lib().hs_prim_label(prim_id(prim), num_iters, buf, 128)
+    return buf.value.decode()
+
+
+def is_barrier(prim) -> bool:
+    return prim_id(prim) <= 3
+
+
+def is_semaphore(prim) -> bool:
+    p = prim_id(prim)
+    return 8 <= p <= 15 or 24 <= p <= 31
+
+
+def sem_count(prim) -> int:
+    name = prim_name(prim_id(prim))
+    for n in ("120", "10", "2", "1"):
+        if ("Sem" in name) and name.endswith(n):
+            return int(n)
+    return 0
+
+
+@dataclass
+class RunConfig:
+    """One run: `repeats` launches of `num_tbs` TBs x `threads` threads, each TB
+    doing `num_iters` critical sections (or barrier episodes) of `num_ldst`
+    loads/stores per thread.  Defaults are the reference's (T=32, 10 repeats)."""
+    prim: object = "faMutex"
+    num_ldst: int = 10
+    num_tbs: int = 8
+    num_iters: int = 100
+    threads: int = 32
+    repeats: int = 10
+    mode: object = "ref"
+    nsm: int = 0
+    backoff_min_ns: int = 1
+    backoff_max_ns: int = 1024
+    backoff_unit_ns: int = 0
+    timeout_ns: int = 0
+    skip_tb: int = -1
+    flags: int = 0
+
+    def to_c(self) -> _RunConfig:
+        mode = _MODES[self.mode] if isinstance(self.mode, str) else int(self.mode)
+        return _RunConfig(prim_id(self.prim), self.num_ldst, self.num_tbs, self.num_iters, self.threads,
+                          self.repeats, mode, self.nsm, self.backoff_min_ns, self.backoff_max_ns,
+                          self.backoff_unit_ns, self.timeout_ns, self.skip_tb, self.flags)
+
+
+@dataclass
+class RunResult:
+    status: int
+    dev_error_bits: int
+    dev_error_site: int
+    elapsed_ms: float
+    avg_ms: float
+    h2d_ms: float
+    d2h_ms: float
+    ops: int
+    launches: int
+
+    @property
+    def ops_per_s(self) -> float:
+        return self.ops / (self.elapsed_ms * 1e-3) if self.elapsed_ms > 0 else float("inf")
+
+
+def storage_words(cfg: RunConfig, nsm: int = 0) -> int:
+    w = ctypes.c_size_t()
+    c = cfg.to_c()
+    s = lib().hs_storage_words(ctypes.byref(c), nsm, ctypes.byref(w))
+    if s:
+        raise _err(s)
+    return int(w.value)
+
+
+def expected_storage(cfg: RunConfig, init, nsm: int = 0):
+    """Expected final storage (numpy uint32) from the initial contents."""
+    import numpy as np
+    init = np.ascontiguousarray(init, dtype=np.uint32)
+    out = np.empty_like(init)
+    c = cfg.to_c()
+    s = lib().hs_expected_storage(ctypes.byref(c), nsm, init.ctypes.data, out.ctypes.data, init.size)
+    if s:
+        raise _err(s)
+    return out
+
+
+def _context():
+    global _ctx
+    if _ctx is None:
+        h = ctypes.c_void_p()
+        s = lib().hs_ctx_create(0, ctypes.byref(h))
+        if s:
+            raise _err(s)
+        _ctx = h
+    return _ctx
+
+
+def run(cfg: RunConfig, storage, stream: Optional[int] = None, check: bool = True) -> RunResult:
+    """Run one primitive on `storage`: a numpy uint32/float32 array (host; copied
+    in and out inside the call) or a CUDA tensor (device; used in place).
+    `stream` is a raw cudaStream_t (defaults to torch's current stream for
+    tensors, the legacy default stream otherwise)."""
+    c = cfg.to_c()
+    need = storage_words(cfg)
+    on_device = 0
+    if hasattr(storage, "data_ptr"):  # torch tensor
+        if not storage.is_cuda:
+            raise ValueError("torch storage must be a CUDA tensor (use numpy for host storage)")
+        if storage.numel() * storage.element_size() < need * 4 or storage.element_size() != 4:
+            raise ValueError("storage needs %d 32-bit words" % need)
+        if not storage.is_contiguous():
+            raise ValueError("storage must be contiguous")
+        ptr = storage.data_ptr()
+        on_device = 1
+        if stream is None:
+            import torch
+            stream = torch.cuda.current_stream(storage.device).cuda_stream
+    else:
+        import numpy as np
+        if not isinstance(storage, np.ndarray) or storage.dtype.itemsize != 4 or not storage.flags.c_contiguous:
+            raise ValueError("host storage must be a contiguous numpy array of 32-bit words")
+        if storage.size < need:
+            raise ValueError("storage needs %d 32-bit words" % need)
+        ptr = storage.ctypes.data
+    r = _RunResult()
+    s = lib().hs_run(_context(), ctypes.byref(c), ctypes.c_void_p(ptr), on_device,
+                     ctypes.c_void_p(stream or 0), ctypes.byref(r))
+    res = RunResult(r.status, r.dev_error_bits, r.dev_error_site, r.elapsed_ms, r.avg_ms, r.h2d_ms, r.d2h_ms,
+                    r.ops, r.launches)
+    if check and s:
+        raise _err(s)
+    return res

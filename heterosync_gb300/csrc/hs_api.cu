@@ -1,0 +1,575 @@
+// hs_api.cu -- host runtime behind include/hs/hs.h: name table, storage sizing,
+// lock-state allocation and initialisation, launches, timing, status readback,
+// and the reference's host API (cudaLocksInit & co.).
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "hs_internal.h"
+#include "../../include/hs/hs.h"
+#include "../../include/hs/hs_device.cuh"
+
+namespace hs {
+using KernelFn = void (*)(RunDesc);
+KernelFn syncprim_kernel(int prim, int mode, int threads);
+cudaError_t launch_ring_init(unsigned* ring, unsigned slots_per_group, unsigned groups, cudaStream_t st);
+cudaError_t launch_fill_lines(unsigned* base, size_t n, size_t stride, unsigned value, cudaStream_t st);
+}  // namespace hs
+
+using namespace hs;
+
+static thread_local std::string g_err;
+static std::atomic<unsigned long long> g_launches{0};
+
+void hs_note_launches(unsigned n) { g_launches += n; }
+
+static int set_cuda_err(cudaError_t e, const char* what) {
+  g_err = std::string(what) + ": " + cudaGetErrorString(e);
+  return HS_ECUDA;
+}
+#define HS_CK(call)                                   \
+  do {                                                \
+    cudaError_t e_ = (call);                          \
+    if (e_ != cudaSuccess) return set_cuda_err(e_, #call); \
+  } while (0)
+
+extern "C" int hs_version(void) { return 1; }
+extern "C" const char* hs_last_error(void) { return g_err.c_str(); }
+extern "C" const char* hs_status_string(int s) {
+  switch (s) {
+    case HS_OK: return "ok";
+    case HS_EINVAL: return "invalid argument";
+    case HS_ETIMEDOUT: return "device wait timed out";
+    case HS_ENORES: return "not enough resources (co-residency or memory)";
+    case HS_ECUDA: return "CUDA error";
+    case HS_ENODEV: return "no CUDA device";
+    case HS_EMISMATCH: return "results differ from expected";
+    default: return "unknown status";
+  }
+}
+extern "C" unsigned long long hs_launch_count(void) { return g_launches.load(); }
+
+extern "C" int hs_device_info(int device, int* nsm, int* cc_major, int* cc_minor, int* max_tpb) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    g_err = "no CUDA device";
+    return HS_ENODEV;
+  }
+  if (device < 0 || device >= n) return HS_EINVAL;
+  cudaDeviceProp p;
+  HS_CK(cudaGetDeviceProperties(&p, device));
+  if (nsm) *nsm = p.multiProcessorCount;
+  if (cc_major) *cc_major = p.major;
+  if (cc_minor) *cc_minor = p.minor;
+  if (max_tpb) *max_tpb = p.maxThreadsPerBlock;
+  return HS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Names and labels: main.cu:1224-1256 (names), 1352-1451 (labels, including the
+// reference's "002" printed for the 120-count spin semaphores).
+// ---------------------------------------------------------------------------
+struct PrimInfo {
+  int id;
+  const char* name;
+  const char* label;  // printf format; semaphores take (count, iters)
+  int label_count;    // semaphore count printed in the label
+  int sem_count;
+};
+static const PrimInfo kPrims[] = {
+    {0, "atomicTreeBarrUniq", "atomic_tree_barrier_%03d", 0, 0},
+    {1, "atomicTreeBarrUniqLocalExch", "atomic_tree_barrier_localExch_%03d", 0, 0},
+    {2, "lfTreeBarrUniq", "fbs_tree_barrier_%03d", 0, 0},
+    {3, "lfTreeBarrUniqLocalExch", "fbs_tree_barrier_localExch_%03d", 0, 0},
+    {4, "spinMutex", "spin_lock_mutex_%03d", 0, 0},
+    {5, "spinMutexEBO", "ebo_mutex_%03d", 0, 0},
+    {6, "sleepMutex", "sleeping_mutex_%03d", 0, 0},
+    {7, "faMutex", "fetchadd_mutex_%03d", 0, 0},
+    {8, "spinSem1", "spin_lock_sem_%03d_%03d", 1, 1},
+    {9, "spinSem2", "spin_lock_sem_%03d_%03d", 2, 2},
+    {10, "spinSem10", "spin_lock_sem_%03d_%03d", 10, 10},
+    {11, "spinSem120", "spin_lock_sem_%03d_%03d", 2, 120},
+    {12, "spinSemEBO1", "ebo_sem_%03d_%03d", 1, 1},
+    {13, "spinSemEBO2", "ebo_sem_%03d_%03d", 2, 2},
+    {14, "spinSemEBO10", "ebo_sem_%03d_%03d", 10, 10},
+    {15, "spinSemEBO120", "ebo_sem_%03d_%03d", 120, 120},
+    {20, "spinMutexUniq", "spin_lock_mutex_uniq_%03d", 0, 0},
+    {21, "spinMutexEBOUniq", "ebo_mutex_uniq_%03d", 0, 0},
+    {22, "sleepMutexUniq", "sleeping_mutex_uniq_%03d", 0, 0},
+    {23, "faMutexUniq", "fetchadd_mutex_uniq_%03d", 0, 0},
+    {24, "spinSemUniq1", "spin_lock_sem_uniq_%03d_%03d", 1, 1},
+    {25, "spinSemUniq2", "spin_lock_sem_uniq_%03d_%03d", 2, 2},
+    {26, "spinSemUniq10", "spin_lock_sem_uniq_%03d_%03d", 10, 10},
+    {27, "spinSemUniq120", "spin_lock_sem_uniq_%03d_%03d", 2, 120},
+    {28, "spinSemEBOUniq1", "ebo_sem_uniq_%03d_%03d", 1, 1},
+    {29, "spinSemEBOUniq2", "ebo_sem_uniq_%03d_%03d", 2, 2},
+    {30, "spinSemEBOUniq10", "ebo_sem_uniq_%03d_%03d", 10, 10},
+    {31, "spinSemEBOUniq120", "ebo_sem_uniq_%03d_%03d", 120, 120},
+};
+static const PrimInfo* find_prim(int id) {
+  for (const auto& p : kPrims)
+    if (p.id == id) return &p;
+  return nullptr;
+}
+extern "C" int hs_prim_id(const char* name) {
+  if (!name) return -1;
+  for (const auto& p : kPrims)
+    if (std::strcmp(p.name, name) == 0) return p.id;
+  return -1;
+}
+extern "C" const char* hs_prim_name(int prim) {
+  const PrimInfo* p = find_prim(prim);
+  return p ? p->name : nullptr;
+}
+extern "C" int hs_prim_label(int prim, int iters, char* buf, int n) {
+  const PrimInfo* p = find_prim(prim);
+  if (!p) return -1;
+  if (p->label_count) return std::snprintf(buf, n, p->label, p->label_count, iters);
+  return std::snprintf(buf, n, p->label, iters);
+}
+extern "C" int hs_prim_sem_count(int prim) {
+  const PrimInfo* p = find_prim(prim);
+  return p ? p->sem_count : 0;
+}
+
+static bool is_barrier(int prim) { return prim >= 0 && prim <= 3; }
+static bool is_gmutex(int prim) { return prim >= 4 && prim <= 7; }
+static bool is_gsem(int prim) { return prim >= 8 && prim <= 15; }
+static bool is_umutex(int prim) { return prim >= 20 && prim <= 23; }
+static bool is_usem(int prim) { return prim >= 24 && prim <= 31; }
+
+// numLocsMult: main.cu:1283-1301.
+static long long locs_mult(int prim, int num_tbs, int nsm) {
+  if (is_barrier(prim) || is_usem(prim)) return num_tbs;
+  if (is_gmutex(prim)) return 1;
+  if (is_gsem(prim)) return ceil_div(num_tbs, nsm);
+  if (is_umutex(prim)) return std::min(num_tbs, nsm);
+  return -1;
+}
+
+static int device_nsm(int nsm_cfg) {
+  if (nsm_cfg > 0) return nsm_cfg;
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return -1; }
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) { cudaGetLastError(); return -1; }
+  return n;
+}
+
+static int validate(const hs_run_config* c, int nsm) {
+  if (!c) { g_err = "null config"; return HS_EINVAL; }
+  if (!find_prim(c->prim)) { g_err = "unknown primitive id"; return HS_EINVAL; }
+  if (c->num_ldst <= 0 || c->num_tbs <= 0 || c->num_iters < 0 || c->repeats < 0) {
+    g_err = "numLdSt and numTBs must be positive, numCSIters and repeats non-negative";
+    return HS_EINVAL;
+  }
+  if (c->threads < 16 || c->threads > 1024 || (c->threads % 16) != 0) {
+    g_err = "threads per TB must be a multiple of 16 in [16, 1024]";
+    return HS_EINVAL;
+  }
+  if (nsm <= 0) { g_err = "NUM_SM must be positive"; return HS_EINVAL; }
+  if (c->mode == HS_MODE_SLICE && !(is_gmutex(c->prim) || is_umutex(c->prim))) {
+    g_err = "HS_MODE_SLICE is defined for the mutex primitives only";
+    return HS_EINVAL;
+  }
+  if (c->mode < 0 || c->mode > 2) { g_err = "unknown mode"; return HS_EINVAL; }
+  if (c->backoff_max_ns && (c->backoff_max_ns & (c->backoff_max_ns - 1))) {
+    g_err = "backoff_max_ns must be a power of two";
+    return HS_EINVAL;
+  }
+  return HS_OK;
+}
+
+extern "C" int hs_storage_words(const hs_run_config* c, int nsm, size_t* words) {
+  nsm = device_nsm(nsm > 0 ? nsm : (c ? c->nsm : 0));
+  int v = validate(c, nsm);
+  if (v) return v;
+  if (c->mode == HS_MODE_SLICE) *words = (size_t)c->num_tbs * c->num_ldst;
+  else *words = (size_t)locs_mult(c->prim, c->num_tbs, nsm) * c->threads * (c->num_ldst + 1);
+  return HS_OK;
+}
+
+extern "C" void hs_run_config_default(hs_run_config* c) {
+  std::memset(c, 0, sizeof(*c));
+  c->prim = 7;
+  c->num_ldst = 10;
+  c->num_tbs = 8;
+  c->num_iters = 100;
+  c->threads = 32;
+  c->repeats = 10;
+  c->mode = HS_MODE_REF;
+  c->nsm = 0;
+  c->backoff_min_ns = 1;
+  c->backoff_max_ns = 1024;
+  c->backoff_unit_ns = 0;
+  c->timeout_ns = 0;
+  c->skip_tb = -1;
+  c->flags = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Closed form of the reference golden (main.cu:1633-1788): the golden applies,
+// per repeat and iteration, one line shift to a set of chunks; the only thing
+// that matters is how many shifts each chunk receives.  Region line n after s
+// shifts holds the initial line max(n - s, 0).
+// ---------------------------------------------------------------------------
+static void shift_counts(const hs_run_config* c, int nsm, std::vector<unsigned long long>& cnt) {
+  const long long nchunks = locs_mult(c->prim, c->num_tbs, nsm);
+  cnt.assign((size_t)nchunks, 0ull);
+  const unsigned long long RI = (unsigned long long)c->repeats * (unsigned long long)c->num_iters;
+  const int G = c->num_tbs;
+  if (is_barrier(c->prim)) {
+    const int nb = std::min(G, nsm);
+    const int k = ceil_div(G, nsm);  // numTBs_perSM as main.cu:1219 computes it
+    (void)nb;
+    const bool exch = (c->prim == 1 || c->prim == 3) && k > 1;
+    for (auto& x : cnt) x = RI * (exch ? 2ull : 1ull);
+  } else if (is_gmutex(c->prim)) {
+    cnt[0] = RI * (unsigned long long)G;
+  } else if (is_gsem(c->prim)) {
+    const int numSM = std::min(G, nsm);
+    const int k = ceil_div(G, numSM);
+    unsigned long long writers = 0;
+    for (int tb = 0; tb < G; ++tb)
+      if (tb / numSM == (tb % numSM) % k) ++writers;
+    for (auto& x : cnt) x = RI * writers;
+  } else if (is_umutex(c->prim)) {
+    for (int b = 0; b < G; ++b) cnt[(size_t)(b % nsm)] += RI;
+  } else {
+    for (auto& x : cnt) x = RI;
+  }
+}
+
+extern "C" int hs_expected_storage(const hs_run_config* c, int nsm, const uint32_t* init, uint32_t* out,
+                                   size_t words) {
+  nsm = device_nsm(nsm > 0 ? nsm : (c ? c->nsm : 0));
+  int v = validate(c, nsm);
+  if (v) return v;
+  size_t need = 0;
+  hs_storage_words(c, nsm, &need);
+  if (words < need || !init || !out) { g_err = "storage too small"; return HS_EINVAL; }
+  const int L = c->num_ldst;
+  if (c->mode == HS_MODE_SLICE) {
+    const uint32_t add = (uint32_t)((unsigned long long)c->repeats * c->num_iters);
+    for (size_t i = 0; i < need; ++i) out[i] = init[i] + add;
+    return HS_OK;
+  }
+  std::vector<unsigned long long> cnt;
+  shift_counts(c, nsm, cnt);
+  const size_t cw = (size_t)c->threads * (L + 1);
+  const int regions = c->threads / 16;
+  for (size_t ch = 0; ch < cnt.size(); ++ch) {
+    const unsigned long long s = cnt[ch];
+    for (int h = 0; h < regions; ++h) {
+      const size_t base = ch * cw + (size_t)h * 16 * (L + 1);
+      for (int n = 0; n <= L; ++n) {
+        for (int o = 0; o < 16; ++o) {
+          const size_t at = base + (size_t)n * 16 + o;
+          if (c->mode == HS_MODE_REF) {
+            const long long src = (unsigned long long)n > s ? (long long)(n - (long long)s) : 0;
+            out[at] = init[base + (size_t)src * 16 + o];
+          } else {
+            out[at] = n == 0 ? init[at] : init[at] + (uint32_t)s;
+          }
+        }
+      }
+    }
+  }
+  return HS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Context: cached device buffers for lock state, rings, status, staging.
+// ---------------------------------------------------------------------------
+struct hs_ctx {
+  int device = 0;
+  int nsm = 0;
+  int max_tpb = 1024;
+  void* locks = nullptr;
+  size_t locks_cap = 0;
+  void* ring = nullptr;
+  size_t ring_cap = 0;
+  unsigned* status = nullptr;
+  void* sink = nullptr;
+  size_t sink_cap = 0;
+  void* staging = nullptr;
+  size_t staging_cap = 0;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+static int ensure(void** p, size_t* cap, size_t bytes) {
+  if (*cap >= bytes) return HS_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    g_err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+    return HS_ENORES;
+  }
+  *cap = bytes;
+  return HS_OK;
+}
+
+extern "C" int hs_ctx_create(int device, hs_ctx** out) {
+  if (!out) return HS_EINVAL;
+  int nsm = 0, tpb = 0;
+  int s = hs_device_info(device, &nsm, nullptr, nullptr, &tpb);
+  if (s) return s;
+  HS_CK(cudaSetDevice(device));
+  hs_ctx* c = new hs_ctx();
+  c->device = device;
+  c->nsm = nsm;
+  c->max_tpb = tpb;
+  cudaError_t e = cudaMalloc(&c->status, 256);
+  if (e != cudaSuccess) { delete c; return set_cuda_err(e, "cudaMalloc(status)"); }
+  for (auto& ev : c->ev) {
+    e = cudaEventCreate(&ev);
+    if (e != cudaSuccess) { delete c; return set_cuda_err(e, "cudaEventCreate"); }
+  }
+  *out = c;
+  return HS_OK;
+}
+
+extern "C" int hs_ctx_destroy(hs_ctx* c) {
+  if (!c) return HS_EINVAL;
+  cudaFree(c->locks);
+  cudaFree(c->ring);
+  cudaFree(c->status);
+  cudaFree(c->sink);
+  cudaFree(c->staging);
+  for (auto& ev : c->ev)
+    if (ev) cudaEventDestroy(ev);
+  delete c;
+  return HS_OK;
+}
+
+static Layout make_layout(const hs_run_config* c, int nsm) {
+  Layout L{};
+  const int G = c->num_tbs;
+  const int nb = std::min(G, nsm);
+  L.groups = std::max(nsm, 1);
+  const int kmax = ceil_div(G, nb) + 1;
+  L.l_glob = 0;
+  L.l_gflag = 4;
+  const int gf_lines = ceil_div(L.groups, kLineWords);
+  L.l_grp = L.l_gflag + gf_lines;
+  L.l_lflag = L.l_grp + 4 * L.groups;
+  L.lflag_lines = ceil_div(kmax, kLineWords);
+  L.lines = L.l_lflag + L.groups * L.lflag_lines;
+  const int ring_groups = is_umutex(c->prim) ? nsm : 1;
+  L.ring_words = (size_t)ring_groups * ((size_t)G + 1) * kRingStride;
+  return L;
+}
+
+// Prepare descriptor + lock state for a run (shared with the batch path).
+int hs_prepare_run(hs_ctx* ctx, const hs_run_config* c, int nsm, void* dev_storage, cudaStream_t st, RunDesc* d,
+                   bool init_state) {
+  const Layout lay = make_layout(c, nsm);
+  int s;
+  if ((s = ensure(&ctx->locks, &ctx->locks_cap, (size_t)lay.lines * kLineWords * 4))) return s;
+  if ((s = ensure(&ctx->ring, &ctx->ring_cap, lay.ring_words * 4))) return s;
+  if ((s = ensure(&ctx->sink, &ctx->sink_cap, (size_t)c->num_tbs * 4 + 256))) return s;
+  std::memset(d, 0, sizeof(*d));
+  d->data = static_cast<unsigned*>(dev_storage);
+  d->locks = static_cast<unsigned*>(ctx->locks);
+  d->ring = static_cast<unsigned*>(ctx->ring);
+  d->status = ctx->status;
+  d->sink = static_cast<unsigned*>(ctx->sink);
+  d->prim = c->prim;
+  d->mode = c->mode;
+  d->T = c->threads;
+  d->L = c->num_ldst;
+  d->num_tbs = c->num_tbs;
+  d->iters = c->num_iters;
+  d->nsm = nsm;
+  d->sem_max = (unsigned)hs_prim_sem_count(c->prim) + 1u;
+  d->bo_min = c->backoff_min_ns ? c->backoff_min_ns : 1u;
+  d->bo_max = c->backoff_max_ns ? c->backoff_max_ns : 1024u;
+  d->bo_unit = c->backoff_unit_ns;
+  d->ring_max = (unsigned)c->num_tbs;
+  d->timeout_ns = c->timeout_ns ? c->timeout_ns : 2000000000ull;
+  d->skip_tb = c->skip_tb;
+  d->cluster = 1;
+  d->l_glob = lay.l_glob;
+  d->l_gflag = lay.l_gflag;
+  d->l_grp = lay.l_grp;
+  d->l_lflag = lay.l_lflag;
+  d->lflag_lines = lay.lflag_lines;
+  HS_CK(cudaMemsetAsync(ctx->status, 0, 256, st));
+  if (init_state) {
+    HS_CK(cudaMemsetAsync(ctx->locks, 0, (size_t)lay.lines * kLineWords * 4, st));
+    if (hs_prim_sem_count(c->prim)) {
+      HS_CK(launch_fill_lines(d->locks + (size_t)lay.l_grp * kLineWords, (size_t)lay.groups,
+                              (size_t)4 * kLineWords, d->sem_max, st));
+      hs_note_launches(1);
+    }
+    if (c->prim == 6 || c->prim == 22) {
+      const unsigned groups = c->prim == 22 ? (unsigned)nsm : 1u;
+      HS_CK(launch_ring_init(d->ring, d->ring_max + 1u, groups, st));
+      hs_note_launches(1);
+    }
+  }
+  return HS_OK;
+}
+
+static int read_status(hs_ctx* ctx, cudaStream_t st, hs_run_result* r) {
+  unsigned h[2] = {0, 0};
+  HS_CK(cudaMemcpyAsync(h, ctx->status, sizeof(h), cudaMemcpyDeviceToHost, st));
+  HS_CK(cudaStreamSynchronize(st));
+  r->dev_error_bits = h[0];
+  r->dev_error_site = h[1];
+  if (h[0] & HS_DEV_TIMEOUT) {
+    g_err = "device wait timed out at site " + std::to_string(h[1]);
+    return HS_ETIMEDOUT;
+  }
+  if (h[0]) {
+    g_err = "device error bits " + std::to_string(h[0]);
+    return HS_EMISMATCH;
+  }
+  return HS_OK;
+}
+
+extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c, void* storage, int on_device, void* stream,
+                      hs_run_result* r) {
+  if (!ctx || !c || !storage || !r) { g_err = "null argument"; return HS_EINVAL; }
+  std::memset(r, 0, sizeof(*r));
+  const int nsm = c->nsm > 0 ? c->nsm : ctx->nsm;
+  int s = validate(c, nsm);
+  if (s) return r->status = s;
+  if (c->threads > ctx->max_tpb) { g_err = "threads per TB above the device limit"; return r->status = HS_EINVAL; }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  HS_CK(cudaSetDevice(ctx->device));
+  size_t words = 0;
+  hs_storage_words(c, nsm, &words);
+  const size_t bytes = words * 4;
+
+  KernelFn fn = syncprim_kernel(c->prim, c->mode, c->threads);
+  if (!fn) { g_err = "no kernel for this primitive/mode"; return r->status = HS_EINVAL; }
+  if (is_barrier(c->prim)) {
+    int per_sm = 0;
+    HS_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, c->threads, 0));
+    if ((long long)per_sm * ctx->nsm < c->num_tbs) {
+      g_err = "barrier TBs cannot all be co-resident (" + std::to_string(per_sm) + " per SM x " +
+              std::to_string(ctx->nsm) + " SMs < " + std::to_string(c->num_tbs) + ")";
+      return r->status = HS_ENORES;
+    }
+  }
+
+  void* dev = storage;
+  if (!on_device) {
+    if ((s = ensure(&ctx->staging, &ctx->staging_cap, bytes + 16))) return r->status = s;
+    dev = ctx->staging;
+    HS_CK(cudaEventRecord(ctx->ev[2], st));
+    HS_CK(cudaMemcpyAsync(dev, storage, bytes, cudaMemcpyHostToDevice, st));
+    HS_CK(cudaEventRecord(ctx->ev[3], st));
+  }
+  RunDesc d;
+  if ((s = hs_prepare_run(ctx, c, nsm, dev, st, &d, !(c->flags & HS_RUN_KEEP_STATE)))) return r->status = s;
+
+  HS_CK(cudaEventRecord(ctx->ev[0], st));
+  for (int rep = 0; rep < c->repeats; ++rep) {
+    void* args[] = {&d};
+    HS_CK(cudaLaunchKernel((const void*)fn, dim3(c->num_tbs), dim3(c->threads), args, 0, st));
+    r->launches++;
+    if (c->flags & HS_RUN_SYNC_EACH) HS_CK(cudaStreamSynchronize(st));
+  }
+  HS_CK(cudaEventRecord(ctx->ev[1], st));
+  hs_note_launches(r->launches);
+  if (!on_device) {
+    HS_CK(cudaMemcpyAsync(storage, dev, bytes, cudaMemcpyDeviceToHost, st));
+  }
+  HS_CK(cudaStreamSynchronize(st));
+  HS_CK(cudaEventElapsedTime(&r->elapsed_ms, ctx->ev[0], ctx->ev[1]));
+  if (!on_device) HS_CK(cudaEventElapsedTime(&r->h2d_ms, ctx->ev[2], ctx->ev[3]));
+  r->avg_ms = c->repeats ? r->elapsed_ms / c->repeats : 0.f;
+  r->ops = (unsigned long long)c->num_tbs * c->num_iters * c->repeats;
+  s = read_status(ctx, st, r);
+  return r->status = s;
+}
+
+// ---------------------------------------------------------------------------
+// The reference's host API: cudaLocks.cu:3-95 and the Create functions.
+// ---------------------------------------------------------------------------
+static hs_lock_data* g_lock = nullptr;
+
+extern "C" hs_lock_data* hs_lock_data_get(void) { return g_lock; }
+
+extern "C" int cudaLocksInit(const int maxBlocksPerKernel, const int numMutexes, const int numSemaphores,
+                             const bool pageAlign, const int NUM_SM) {
+  (void)pageAlign;
+  if (maxBlocksPerKernel <= 0 || numMutexes <= 0 || numSemaphores <= 0 || NUM_SM <= 0)
+    return (int)cudaErrorInitializationError;  // cudaLocks.cu:13-15
+  if (g_lock) cudaLocksDestroy();
+  hs_lock_data* L = nullptr;
+  cudaError_t e = cudaMallocHost(&L, sizeof(hs_lock_data));
+  if (e != cudaSuccess) return (int)e;
+  std::memset(L, 0, sizeof(*L));
+  L->maxBufferSize = maxBlocksPerKernel;
+  L->arrayStride = (maxBlocksPerKernel + NUM_SM) / 16 * 16;  // cudaLocks.cu:19
+  L->mutexCount = numMutexes;
+  L->semaphoreCount = numSemaphores;
+  const size_t stride = (size_t)L->arrayStride;
+  if ((e = cudaMalloc(&L->barrierBuffers, 4 * stride * 2)) != cudaSuccess) return (int)e;
+  if ((e = cudaMalloc(&L->mutexBuffers, 4 * stride * numMutexes)) != cudaSuccess) return (int)e;
+  if ((e = cudaMalloc(&L->mutexBufferHeads, 4 * (size_t)numMutexes)) != cudaSuccess) return (int)e;
+  if ((e = cudaMalloc(&L->mutexBufferTails, 4 * (size_t)numMutexes)) != cudaSuccess) return (int)e;
+  if ((e = cudaMalloc(&L->semaphoreBuffers, 4 * 4 * (size_t)numSemaphores)) != cudaSuccess) return (int)e;
+  cudaMemset(L->barrierBuffers, 0, 4 * stride * 2);
+  cudaMemset(L->mutexBufferHeads, 0, 4 * (size_t)numMutexes);
+  cudaMemset(L->mutexBufferTails, 0, 4 * (size_t)numMutexes);
+  cudaMemset(L->semaphoreBuffers, 0, 4 * 4 * (size_t)numSemaphores);
+  // rings: first slot of every ring 1, the rest -1 (cudaLocks.cu:58-65)
+  std::vector<int> ring(stride * numMutexes, -1);
+  for (size_t i = 0; i < ring.size(); i += stride) ring[i] = 1;
+  e = cudaMemcpy(L->mutexBuffers, ring.data(), ring.size() * 4, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return (int)e;
+  e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return (int)e;
+  g_lock = L;
+  return 0;
+}
+
+extern "C" int cudaLocksDestroy(void) {
+  if (!g_lock) return (int)cudaErrorInitializationError;
+  cudaFree(g_lock->barrierBuffers);
+  cudaFree(g_lock->mutexBuffers);
+  cudaFree(g_lock->mutexBufferHeads);
+  cudaFree(g_lock->mutexBufferTails);
+  cudaFree(g_lock->semaphoreBuffers);
+  cudaFreeHost(g_lock);
+  g_lock = nullptr;
+  return 0;
+}
+
+extern "C" int cudaMutexCreateSpin(unsigned int* const h, const int n) { *h = (unsigned)n; return 0; }
+extern "C" int cudaMutexCreateEBO(unsigned int* const h, const int n) { *h = (unsigned)n; return 0; }
+extern "C" int cudaMutexCreateFA(unsigned int* const h, const int n) { *h = (unsigned)n; return 0; }
+extern "C" int cudaMutexCreateSleep(unsigned int* const h, const int n) { *h = (unsigned)n; return 0; }
+
+// Initial words for every SM copy: {count+1, 0, 0, count+1} (cudaLocksSemaphoreSpin.cu:12-22),
+// written with one copy instead of 4*NUM_SM.
+static int sem_create(unsigned int* const h, const int sem, const unsigned count, const int NUM_SM) {
+  if (!g_lock) return (int)cudaErrorInitializationError;
+  if (sem < 0 || (long long)(sem + 1) * NUM_SM > g_lock->semaphoreCount) return (int)cudaErrorInvalidValue;
+  *h = (unsigned)sem;
+  std::vector<unsigned> w((size_t)4 * NUM_SM);
+  for (int id = 0; id < NUM_SM; ++id) {
+    w[4 * id + 0] = count + 1;
+    w[4 * id + 1] = 0;
+    w[4 * id + 2] = 0;
+    w[4 * id + 3] = count + 1;
+  }
+  return (int)cudaMemcpy(g_lock->semaphoreBuffers + (size_t)sem * 4 * NUM_SM, w.data(), w.size() * 4,
+                         cudaMemcpyHostToDevice);
+}
+extern "C" int cudaSemaphoreCreateSpin(unsigned int* const h, const int s, const unsigned int count, const int nsm) {
+  return sem_create(h, s, count, nsm);
+}
+extern "C" int cudaSemaphoreCreateEBO(unsigned int* const h, const int s, const unsigned int count, const int nsm) {
+  return sem_create(h, s, count, nsm);
+}

@@ -1,0 +1,429 @@
+// hs_syncprims.cu -- the SyncPrims kernels (mutexes, semaphores, tree barriers)
+// for sm_103a.
+//
+// Each kernel executes numCSIters iterations per TB of the reference kernel of
+// the same name (heterosync cuda/syncPrims/uvm/main.cu:104-836): acquire,
+// critical section on the shared data, release -- or, for barriers, data
+// access then barrier.  Which TB touches which data, and when, follows the
+// reference exactly, so the final shared data equals the reference's golden.
+//
+// What is different is how each step maps onto the GPU:
+//  * the critical section moves whole 16-byte vectors: all loads of a pass are
+//    issued before any store (one L2 round trip instead of numLdSt dependent
+//    load->store round trips), separated by one CTA barrier;
+//  * lock words are padded to their own 128-byte line;
+//  * one lane polls with ld.acquire and broadcasts with one bar.red;
+//  * releases are single st.release / red.release operations;
+//  * barrier state is generation-valued (no resets) and groups may be uneven;
+//  * every wait is bounded (see hs_device.cuh).
+#include <cuda_runtime.h>
+#include "hs_internal.h"
+#include "../../include/hs/hs_device.cuh"
+
+namespace hs {
+
+// ---------------------------------------------------------------------------
+// Critical-section bodies.  A "chunk" is the data of one reference TB: T/16
+// half-warp regions of (L+1) lines x 16 words (main.cu:60-72, 1304-1308).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ size_t chunk_words(int T, int L) { return (size_t)T * (L + 1); }
+
+// REF: line n+1 <- line n for n = L-1..0 in every region of the chunk.
+// Passes of up to 32 lines go from the top down; each pass loads everything
+// into registers, one CTA barrier, then stores.  Stores of a pass never touch
+// lines a later pass loads, and a later pass only overwrites lines an earlier
+// pass already loaded, so one barrier per pass suffices.
+template <int MAXV>
+__device__ __forceinline__ void cs_ref_shift(unsigned* chunk, int T, int L) {
+  const int R = T >> 4;
+  const int rw4 = (L + 1) * 4;
+  uint4* c4 = reinterpret_cast<uint4*>(chunk);
+  const int lpp = 4 * MAXV;  // lines per pass: MAXV*T items / (R regions * 4 vectors)
+  for (int hi = L; hi > 0; hi -= lpp) {
+    const int lo = hi - lpp > 0 ? hi - lpp : 0;
+    const int per_region = (hi - lo) * 4;
+    const int nitems = R * per_region;
+    uint4 v[MAXV];
+    int idx[MAXV];
+#pragma unroll
+    for (int u = 0; u < MAXV; ++u) {
+      const int t = threadIdx.x + u * T;
+      idx[u] = -1;
+      if (t < nitems) {
+        const int h = t / per_region;
+        idx[u] = h * rw4 + lo * 4 + (t - h * per_region);
+        v[u] = c4[idx[u]];
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < MAXV; ++u)
+      if (idx[u] >= 0) c4[idx[u] + 4] = v[u];
+  }
+}
+
+// INC: every word of lines 1..L of every region gets +1.
+template <int MAXV>
+__device__ __forceinline__ void cs_inc(unsigned* chunk, int T, int L) {
+  const int R = T >> 4;
+  const int rw4 = (L + 1) * 4;
+  const int per_region = L * 4;
+  const int nitems = R * per_region;
+  uint4* c4 = reinterpret_cast<uint4*>(chunk);
+  for (int base = 0; base < nitems; base += MAXV * T) {
+    uint4 v[MAXV];
+    int idx[MAXV];
+#pragma unroll
+    for (int u = 0; u < MAXV; ++u) {
+      const int t = base + threadIdx.x + u * T;
+      idx[u] = -1;
+      if (t < nitems) {
+        const int h = t / per_region;
+        idx[u] = h * rw4 + 4 + (t - h * per_region);
+        v[u] = c4[idx[u]];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < MAXV; ++u)
+      if (idx[u] >= 0) {
+        v[u].x += 1u; v[u].y += 1u; v[u].z += 1u; v[u].w += 1u;
+        c4[idx[u]] = v[u];
+      }
+  }
+}
+
+// SLICE: words [s*L, s*L+L) get +1, one thread per word.
+__device__ __forceinline__ void cs_slice(unsigned* data, int s, int L) {
+  unsigned* p = data + (size_t)s * L;
+  for (int w = threadIdx.x; w < L; w += blockDim.x) p[w] += 1u;
+}
+
+// Semaphore reader: load lines 0..L-1 of the chunk (main.cu:89-100); the loaded
+// values are folded into one word per TB so the loads are not dead.
+__device__ __forceinline__ void cs_read(const unsigned* chunk, int T, int L, unsigned* sink_slot) {
+  const int R = T >> 4;
+  const int rw4 = (L + 1) * 4;
+  const int per_region = L * 4;
+  const int nitems = R * per_region;
+  const uint4* c4 = reinterpret_cast<const uint4*>(chunk);
+  unsigned acc = 0;
+  for (int t = threadIdx.x; t < nitems; t += T) {
+    const int h = t / per_region;
+    const uint4 v = c4[h * rw4 + (t - h * per_region)];
+    acc += v.x ^ v.y ^ v.z ^ v.w;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
+  if ((threadIdx.x & 31) == 0 && acc == 0x9E3779B9u) *sink_slot = acc;  // practically never taken
+}
+
+// Threads per CTA above 512 get a smaller register budget per thread.
+template <bool BIG> struct Bounds { static constexpr int kThreads = BIG ? 1024 : 512; static constexpr int kVec = BIG ? 4 : 8; };
+
+template <int MODE, bool BIG = false>
+__device__ __forceinline__ void cs_chunk(const RunDesc& d, int chunk) {
+  unsigned* c = d.data + (size_t)chunk * chunk_words(d.T, d.L);
+  if constexpr (MODE == M_REF) cs_ref_shift<Bounds<BIG>::kVec>(c, d.T, d.L);
+  else cs_inc<Bounds<BIG>::kVec>(c, d.T, d.L);
+}
+
+__device__ __forceinline__ unsigned* group_line(const RunDesc& d, int g, int k) {
+  return d.locks + (size_t)(d.l_grp + 4 * g + k) * kLineWords;
+}
+
+// ---------------------------------------------------------------------------
+// Mutex kernels: main.cu:317-529.  Global variants: one lock, every TB works on
+// chunk 0.  Uniq variants: lock and chunk per logical SM (blockIdx % NUM_SM).
+// ---------------------------------------------------------------------------
+template <int KIND, bool UNIQ, int MODE, bool BIG>
+__global__ void __launch_bounds__(Bounds<BIG>::kThreads) k_mutex(RunDesc d) {
+  __shared__ int s_slot;
+  const int b = blockIdx.x;
+  const int g = UNIQ ? (b % d.nsm) : 0;
+  unsigned* w0 = group_line(d, g, 0);
+  unsigned* w1 = group_line(d, g, 1);
+  unsigned* w2 = group_line(d, g, 2);
+  unsigned* ring = d.ring + (size_t)g * (d.ring_max + 1) * kRingStride;
+  const unsigned wrap = UNIQ ? 100000000u : 1000000000u;  // cudaLocksMutexFA.cu:24,83
+  const HsEnv env{d.status, d.timeout_ns};
+  // SLICE mode bookkeeping: group members b = g + r*G, r = 0..m-1.
+  const int G = UNIQ ? d.nsm : 1;
+  const int r = b / G;
+  const int m = (d.num_tbs - g + G - 1) / G;
+
+  for (int j = 0; j < d.iters; ++j) {
+    bool ok;
+    int slot = 0;
+    if constexpr (KIND == MK_SPIN) ok = spin_lock<GPU>(w0, env);
+    else if constexpr (KIND == MK_EBO) ok = ebo_lock<GPU>(w0, d.bo_min, d.bo_max, env);
+    else if constexpr (KIND == MK_FA) ok = ticket_lock<GPU>(w0, w1, wrap, d.bo_unit, d.bo_max, env);
+    else {
+      slot = queue_lock<GPU>(w2, ring, kRingStride, d.ring_max, d.bo_unit, env, &s_slot);
+      ok = slot >= 0;
+    }
+    if (!ok) break;
+
+    if constexpr (MODE == M_SLICE) cs_slice(d.data, g + ((r + j) % m) * G, d.L);
+    else cs_chunk<MODE, BIG>(d, g);
+
+    if constexpr (KIND == MK_SPIN || KIND == MK_EBO) spin_unlock<GPU>(w0);
+    else if constexpr (KIND == MK_FA) ticket_unlock<GPU>(w1, wrap);
+    else queue_unlock<GPU>(ring, kRingStride, d.ring_max, (unsigned)slot);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Semaphore kernels: main.cu:533-836.  One writer TB per logical SM
+// (perSM_blockID == smID % numTBs_perSM); the rest are readers.
+// ---------------------------------------------------------------------------
+template <bool EBO, bool UNIQ, int MODE, bool BIG>
+__global__ void __launch_bounds__(Bounds<BIG>::kThreads) k_sem(RunDesc d) {
+  const int b = blockIdx.x;
+  const int Gd = d.num_tbs;
+  const int numSM = Gd < d.nsm ? Gd : d.nsm;
+  const int smID = b % numSM;
+  const int k = ceil_div(Gd, numSM);
+  const int p = b / numSM;
+  const bool writer = (p == smID % k);
+  unsigned* st = group_line(d, UNIQ ? smID : 0, 0);
+  const HsEnv env{d.status, d.timeout_ns};
+  const int rchunk = UNIQ ? b : p;
+
+  for (int i = 0; i < d.iters; ++i) {
+    if (!sem_wait<GPU>(st, writer, d.sem_max, EBO, !UNIQ, d.bo_min, d.bo_max, env)) break;
+    if (writer) {
+      if constexpr (UNIQ) {
+        int cur = b;
+        for (int j = 0; j < k; ++j) {
+          cs_chunk<MODE, BIG>(d, cur);
+          cur = (cur + numSM) % Gd;
+        }
+      } else {
+        for (int j = 0; j < k; ++j) cs_chunk<MODE, BIG>(d, j);
+      }
+    } else {
+      cs_read(d.data + (size_t)rchunk * chunk_words(d.T, d.L), d.T, d.L, d.sink + b);
+    }
+    sem_post<GPU>(st, writer, d.sem_max);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Tree barriers: main.cu:104-315.  Logical SM group g = b % nb (nb = min(numTBs,
+// NUM_SM)), member index r = b / nb, m_g members (uneven groups allowed).
+//
+// Atomic tree (LF == false): per-group counter barrier whose last arriver runs
+// the global counter barrier among the nb groups, then publishes the group
+// generation.  Lock-free tree (LF == true): members publish generation flags,
+// the group's first member scans them and joins a flag barrier among group
+// leaders scanned by group 0's leader, which publishes the global release word.
+// ---------------------------------------------------------------------------
+struct BarState {
+  unsigned lgen;  // group generation (local stage)
+  unsigned ggen;  // global generation
+};
+
+template <bool LF>
+__device__ __forceinline__ bool local_only_barrier(const RunDesc& d, int g, int r, int m, BarState& s,
+                                                   const HsEnv& env) {
+  unsigned* lcount = group_line(d, g, 0);
+  unsigned* lgen = group_line(d, g, 1);
+  unsigned* lgo = group_line(d, g, 2);
+  unsigned* lflags = d.locks + (size_t)(d.l_lflag + g * d.lflag_lines) * kLineWords;
+  int ok = 1;
+  if constexpr (!LF) {
+    if (is_master()) {
+      bool okb = true;
+      counter_barrier<GPU>(lcount, lgen, (unsigned)m, s.lgen, d.bo_unit, env, HS_SITE_BAR_LOCAL,
+                           [] { return true; }, &okb);
+      ok = okb;
+    }
+    s.lgen += 1u;
+    return __syncthreads_or(!ok) == 0;  // non-masters keep ok == 1
+  } else {
+    const unsigned e = s.lgen + 1u;
+    if (r != 0) {
+      if (is_master()) {
+        st_release<GPU>(lflags + r, e);
+        ok = wait_until([&] { return (int)(ld_acquire<GPU>(lgo) - e) >= 0; }, [&] { sleep_ns(d.bo_unit); }, env,
+                        HS_SITE_BAR_GO);
+      }
+      ok = __syncthreads_or(!ok) == 0;
+    } else {
+      ok = scan_flags<GPU>(lflags + 1, (unsigned)(m - 1), e, d.bo_unit, env, HS_SITE_BAR_SCAN);
+      if (ok && is_master()) st_release<GPU>(lgo, e);
+    }
+    s.lgen = e;
+    return ok != 0;
+  }
+}
+
+template <bool LF>
+__device__ __forceinline__ bool tree_barrier(const RunDesc& d, int g, int r, int m, int nb, BarState& s,
+                                             const HsEnv& env) {
+  unsigned* gcount = d.locks + (size_t)(d.l_glob + 0) * kLineWords;
+  unsigned* ggenw = d.locks + (size_t)(d.l_glob + 1) * kLineWords;
+  unsigned* ggo = d.locks + (size_t)(d.l_glob + 2) * kLineWords;
+  unsigned* gflags = d.locks + (size_t)d.l_gflag * kLineWords;
+  int ok = 1;
+  if constexpr (!LF) {
+    if (m == 1) {  // no local stage
+      if (is_master()) {
+        bool okb = true;
+        counter_barrier<GPU>(gcount, ggenw, (unsigned)nb, s.ggen, d.bo_unit, env, HS_SITE_BAR_GLOBAL,
+                             [] { return true; }, &okb);
+        ok = okb;
+      }
+    } else if (is_master()) {
+      unsigned* lcount = group_line(d, g, 0);
+      unsigned* lgen = group_line(d, g, 1);
+      bool okb = true;
+      const unsigned gg = s.ggen;
+      counter_barrier<GPU>(lcount, lgen, (unsigned)m, s.lgen, d.bo_unit, env, HS_SITE_BAR_LOCAL,
+                           [&] {
+                             bool ok2 = true;
+                             counter_barrier<GPU>(gcount, ggenw, (unsigned)nb, gg, d.bo_unit, env,
+                                                  HS_SITE_BAR_GLOBAL, [] { return true; }, &ok2);
+                             return ok2;
+                           },
+                           &okb);
+      ok = okb;
+    }
+    if (m != 1) s.lgen += 1u;
+    s.ggen += 1u;
+    return __syncthreads_or(!ok) == 0;
+  } else {
+    const unsigned e = s.lgen + 1u;
+    const unsigned E = s.ggen + 1u;
+    unsigned* lgo = group_line(d, g, 2);
+    unsigned* lflags = d.locks + (size_t)(d.l_lflag + g * d.lflag_lines) * kLineWords;
+    if (r != 0) {
+      if (is_master()) {
+        st_release<GPU>(lflags + r, e);
+        ok = wait_until([&] { return (int)(ld_acquire<GPU>(lgo) - e) >= 0; }, [&] { sleep_ns(d.bo_unit); }, env,
+                        HS_SITE_BAR_GO);
+      }
+      ok = __syncthreads_or(!ok) == 0;
+    } else {
+      if (m > 1) ok = scan_flags<GPU>(lflags + 1, (unsigned)(m - 1), e, d.bo_unit, env, HS_SITE_BAR_SCAN);
+      if (ok && is_master()) st_release<GPU>(gflags + g, E);
+      if (g == 0) {
+        if (ok) ok = scan_flags<GPU>(gflags, (unsigned)nb, E, d.bo_unit, env, HS_SITE_BAR_SCAN);
+        if (ok && is_master()) st_release<GPU>(ggo, E);
+      } else if (is_master() && ok) {
+        ok = wait_until([&] { return (int)(ld_acquire<GPU>(ggo) - E) >= 0; }, [&] { sleep_ns(d.bo_unit); }, env,
+                        HS_SITE_BAR_GO);
+      }
+      if (is_master() && ok && m > 1) st_release<GPU>(lgo, e);
+      ok = __syncthreads_or(!ok) == 0;
+    }
+    if (m > 1) s.lgen = e;
+    s.ggen = E;
+    return ok != 0;
+  }
+}
+
+template <bool LF, bool EXCH, int MODE, bool BIG>
+__global__ void __launch_bounds__(Bounds<BIG>::kThreads) k_barrier(RunDesc d) {
+  const int b = blockIdx.x;
+  const int Gd = d.num_tbs;
+  const int nb = Gd < d.nsm ? Gd : d.nsm;
+  const int g = b % nb;
+  const int r = b / nb;
+  const int m = (Gd - g + nb - 1) / nb;
+  const int kmax = ceil_div(Gd, nb);
+  const HsEnv env{d.status, d.timeout_ns};
+
+  // Generations at kernel start (state persists across launches).
+  __shared__ BarState s_init;
+  if (is_master()) {
+    s_init.lgen = LF ? ld_relaxed<GPU>(group_line(d, g, 2)) : ld_relaxed<GPU>(group_line(d, g, 1));
+    s_init.ggen = LF ? ld_relaxed<GPU>(d.locks + (size_t)(d.l_glob + 2) * kLineWords)
+                     : ld_relaxed<GPU>(d.locks + (size_t)(d.l_glob + 1) * kLineWords);
+  }
+  __syncthreads();
+  BarState s = s_init;
+
+  int cur = b;
+  for (int i = 0; i < d.iters; ++i) {
+    cs_chunk<MODE, BIG>(d, cur);
+    if (b == d.skip_tb) return;  // fault injection: this TB never arrives
+    if (EXCH && kmax > 1) {
+      if (!local_only_barrier<LF>(d, g, r, m, s, env)) return;
+      cur = (cur + nb) % Gd;
+      cs_chunk<MODE, BIG>(d, cur);
+    }
+    if (!tree_barrier<LF>(d, g, r, m, nb, s, env)) return;
+    cur = (cur + 1) % Gd;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Ring initialisation: slot 0 of every group's ring = 1, the rest = -1
+// (cudaLocks.cu:58-65).
+// ---------------------------------------------------------------------------
+__global__ void k_ring_init(unsigned* ring, unsigned slots_per_group, unsigned groups) {
+  const size_t n = (size_t)slots_per_group * groups;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    ring[i * kRingStride] = (i % slots_per_group == 0) ? 1u : 0xFFFFFFFFu;
+}
+
+// ---------------------------------------------------------------------------
+// Host-side dispatch.
+// ---------------------------------------------------------------------------
+using KernelFn = void (*)(RunDesc);
+
+template <int MODE, bool BIG>
+static KernelFn pick(int prim) {
+  if constexpr (MODE != M_SLICE) {
+    switch (prim) {
+      case P_ATOMIC_TREE: return k_barrier<false, false, MODE, BIG>;
+      case P_ATOMIC_TREE_EXCH: return k_barrier<false, true, MODE, BIG>;
+      case P_LF_TREE: return k_barrier<true, false, MODE, BIG>;
+      case P_LF_TREE_EXCH: return k_barrier<true, true, MODE, BIG>;
+      default: break;
+    }
+    if (prim >= P_SPIN_SEM1 && prim <= P_SPIN_SEM120) return k_sem<false, false, MODE, BIG>;
+    if (prim >= P_EBO_SEM1 && prim <= P_EBO_SEM120) return k_sem<true, false, MODE, BIG>;
+    if (prim >= P_SPIN_SEM_UNIQ1 && prim <= P_SPIN_SEM_UNIQ120) return k_sem<false, true, MODE, BIG>;
+    if (prim >= P_EBO_SEM_UNIQ1 && prim <= P_EBO_SEM_UNIQ120) return k_sem<true, true, MODE, BIG>;
+  }
+  switch (prim) {
+    case P_SPIN_MUTEX: return k_mutex<MK_SPIN, false, MODE, BIG>;
+    case P_EBO_MUTEX: return k_mutex<MK_EBO, false, MODE, BIG>;
+    case P_SLEEP_MUTEX: return k_mutex<MK_SLEEP, false, MODE, BIG>;
+    case P_FA_MUTEX: return k_mutex<MK_FA, false, MODE, BIG>;
+    case P_SPIN_MUTEX_UNIQ: return k_mutex<MK_SPIN, true, MODE, BIG>;
+    case P_EBO_MUTEX_UNIQ: return k_mutex<MK_EBO, true, MODE, BIG>;
+    case P_SLEEP_MUTEX_UNIQ: return k_mutex<MK_SLEEP, true, MODE, BIG>;
+    case P_FA_MUTEX_UNIQ: return k_mutex<MK_FA, true, MODE, BIG>;
+    default: return nullptr;
+  }
+}
+
+KernelFn syncprim_kernel(int prim, int mode, int threads) {
+  const bool big = threads > 512;
+  switch (mode) {
+    case M_REF: return big ? pick<M_REF, true>(prim) : pick<M_REF, false>(prim);
+    case M_INC: return big ? pick<M_INC, true>(prim) : pick<M_INC, false>(prim);
+    case M_SLICE: return big ? pick<M_SLICE, true>(prim) : pick<M_SLICE, false>(prim);
+    default: return nullptr;
+  }
+}
+
+__global__ void k_fill_lines(unsigned* base, size_t n, size_t stride, unsigned value) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    base[i * stride] = value;
+}
+
+cudaError_t launch_fill_lines(unsigned* base, size_t n, size_t stride, unsigned value, cudaStream_t st) {
+  k_fill_lines<<<(unsigned)((n + 255) / 256 > 152 ? 152 : (n + 255) / 256), 256, 0, st>>>(base, n, stride, value);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ring_init(unsigned* ring, unsigned slots_per_group, unsigned groups, cudaStream_t st) {
+  k_ring_init<<<152, 256, 0, st>>>(ring, slots_per_group, groups);
+  return cudaGetLastError();
+}
+
+}  // namespace hs

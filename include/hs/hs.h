@@ -1,0 +1,155 @@
+/* hs.h -- C ABI of the GB300-native HeteroSync hot path (libhsgb300.so).
+ *
+ * Plain C types only.  Every function returns an int status (HS_OK == 0) unless
+ * stated otherwise.  Device memory pointers are plain `void*`; streams are the
+ * `cudaStream_t` value cast to `void*` (NULL = the legacy default stream).
+ *
+ * Two groups of entry points:
+ *  1. The reference's own host API, same names and arguments (so a program
+ *     written against heterosync's cudaLocks.h links against this library):
+ *     cudaLocksInit / cudaLocksDestroy / cudaMutexCreate* / cudaSemaphoreCreate*.
+ *  2. hs_* entry points that replace the reference's per-primitive host
+ *     launch wrappers (invoke*, cuda/syncPrims/uvm/main.cu:838-1128) and its
+ *     command line (main.cu:1130-1821), plus the batch, serving and probe paths
+ *     this build adds.
+ */
+#ifndef HS_H_
+#define HS_H_
+
+#include <stddef.h>
+#include <stdint.h>
+#include <stdbool.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------- */
+enum {
+  HS_OK = 0,
+  HS_EINVAL = 1,       /* bad argument (sizes, unknown primitive, mode not supported) */
+  HS_ETIMEDOUT = 2,    /* a bounded device wait ran out (device status has the site) */
+  HS_ENORES = 3,       /* the launch cannot be co-resident (barriers) or memory is short */
+  HS_ECUDA = 4,        /* a CUDA runtime call failed (hs_last_error() has the text) */
+  HS_ENODEV = 5,       /* no CUDA device */
+  HS_EMISMATCH = 6     /* a self-check found results that differ from the expected ones */
+};
+
+/* ---- data modes ------------------------------------------------------------ */
+enum {
+  HS_MODE_REF = 0,     /* reference critical section: one-line copy shift of 32-bit words */
+  HS_MODE_INC = 1,     /* same locations, every written word += 1 (exact count check) */
+  HS_MODE_SLICE = 2    /* uint32[numTBs*numLdSt]; TB b, iteration j: slice (b+j) mod numTBs += 1 (mutexes) */
+};
+
+/* ---- run flags --------------------------------------------------------------- */
+enum {
+  HS_RUN_SYNC_EACH = 1,   /* host-synchronise after every launch, as main.cu:844-854 does */
+  HS_RUN_KEEP_STATE = 2   /* do not re-initialise lock state before the repeats */
+};
+
+/* One run of one SyncPrims primitive: `repeats` launches of `num_tbs` TBs of
+ * `threads` threads, each TB doing `num_iters` critical sections / episodes. */
+typedef struct hs_run_config {
+  int prim;             /* reference syncPrim id, see hs_prim_id() */
+  int num_ldst;         /* <numLdSt> */
+  int num_tbs;          /* <numTBs> */
+  int num_iters;        /* <numCSIters> */
+  int threads;          /* threads per TB (reference: 32, main.cu:8); multiple of 16, <= 1024 */
+  int repeats;          /* launches (reference: NUM_REPEATS = 10, main.cu:21) */
+  int mode;             /* HS_MODE_* */
+  int nsm;              /* NUM_SM used in the reference index math; 0 = device SM count */
+  unsigned backoff_min_ns;   /* EBO start (reference 1) */
+  unsigned backoff_max_ns;   /* EBO cap, power of two (reference MAX_BACKOFF = 1024) */
+  unsigned backoff_unit_ns;  /* ticket-lock per-position sleep / poll sleep (0 = spin) */
+  unsigned long long timeout_ns; /* per-wait limit, 0 = 2 s */
+  int skip_tb;          /* fault injection for barriers: this TB never arrives (-1 = none) */
+  int flags;            /* HS_RUN_* */
+} hs_run_config;
+
+typedef struct hs_run_result {
+  int status;                   /* HS_OK, HS_ETIMEDOUT, ... */
+  unsigned dev_error_bits;      /* device status word 0 */
+  unsigned dev_error_site;      /* device status word 1 (wait site) */
+  float elapsed_ms;             /* device time of all launches (CUDA events on the launch stream) */
+  float avg_ms;                 /* elapsed_ms / repeats: the reference's "average" */
+  float h2d_ms, d2h_ms;         /* storage copies when storage is host memory */
+  unsigned long long ops;       /* num_tbs * num_iters * repeats */
+  unsigned launches;            /* kernels launched by this call */
+} hs_run_result;
+
+typedef struct hs_ctx hs_ctx;
+
+/* ---- library / device -------------------------------------------------------- */
+int hs_version(void);
+const char* hs_last_error(void);
+const char* hs_status_string(int status);
+/* Multiprocessor count, compute capability and max threads/block of `device`. */
+int hs_device_info(int device, int* nsm, int* cc_major, int* cc_minor, int* max_threads_per_block);
+/* Total kernels this library has launched in this process (all entry points). */
+unsigned long long hs_launch_count(void);
+
+/* ---- primitive names (main.cu:1224-1256) ------------------------------------- */
+/* Reference name -> syncPrim id (0-15, 20-31); -1 if unknown. */
+int hs_prim_id(const char* name);
+/* syncPrim id -> reference name; NULL if unknown. */
+const char* hs_prim_name(int prim);
+/* The label the reference prints before timing (main.cu:1352-1451), e.g.
+ * "fetchadd_mutex_100"; returns the length written (snprintf semantics). */
+int hs_prim_label(int prim, int num_iters, char* buf, int buflen);
+/* Semaphore size for semaphore prims (1, 2, 10, 120), 0 otherwise. */
+int hs_prim_sem_count(int prim);
+/* Storage words a run needs (numLocsMult * threads * (numLdSt+1), main.cu:1283-1308;
+ * numTBs * numLdSt for HS_MODE_SLICE). */
+int hs_storage_words(const hs_run_config* cfg, int nsm, size_t* words);
+
+/* ---- runs (replace invoke*, main.cu:838-1128) -------------------------------- */
+int hs_ctx_create(int device, hs_ctx** out);
+int hs_ctx_destroy(hs_ctx* ctx);
+/* Fill *cfg with the reference defaults (threads 32, repeats 10, REF mode, ...). */
+void hs_run_config_default(hs_run_config* cfg);
+/* Run one primitive.  `storage` holds hs_storage_words() 32-bit words, on the
+ * device (storage_on_device != 0) or in host memory (copied in and out inside
+ * the call and timed in h2d_ms / d2h_ms).  Synchronises before returning. */
+int hs_run(hs_ctx* ctx, const hs_run_config* cfg, void* storage, int storage_on_device, void* stream,
+           hs_run_result* result);
+/* Expected final storage of a run, from its initial contents (closed form of
+ * the reference's golden replay, main.cu:1633-1788).  Host arrays. */
+int hs_expected_storage(const hs_run_config* cfg, int nsm, const uint32_t* init, uint32_t* expected, size_t words);
+
+/* ---- the reference's host API (cuda/syncPrims/uvm/cudaLocks.h:4-26) ----------- */
+/* Same field order as cudaLockData_t (cudaLocks.h:4-16). */
+typedef struct hs_lock_data {
+  int maxBufferSize;
+  int arrayStride;
+  int mutexCount;
+  int semaphoreCount;
+  unsigned int* barrierBuffers;
+  int* mutexBuffers;
+  unsigned int* mutexBufferHeads;
+  unsigned int* mutexBufferTails;
+  unsigned int* semaphoreBuffers;
+} hs_lock_data;
+
+/* cudaLocks.cu:3-81.  Returns a cudaError_t value (0 = cudaSuccess). */
+int cudaLocksInit(const int maxBlocksPerKernel, const int numMutexes, const int numSemaphores, const bool pageAlign,
+                  const int NUM_SM);
+/* cudaLocks.cu:83-95 (this one also frees barrierBuffers). */
+int cudaLocksDestroy(void);
+/* The lock data cudaLocksInit filled in (the reference's cpuLockData, pinned host memory). */
+hs_lock_data* hs_lock_data_get(void);
+/* cudaLocksMutexSpin.cu:4, cudaLocksMutexEBO.cu:6, cudaLocksMutexFA.cu:6, cudaLocksMutexSleep.cu:6 */
+int cudaMutexCreateSpin(unsigned int* const handle, const int mutexNumber);
+int cudaMutexCreateEBO(unsigned int* const handle, const int mutexNumber);
+int cudaMutexCreateFA(unsigned int* const handle, const int mutexNumber);
+int cudaMutexCreateSleep(unsigned int* const handle, const int mutexNumber);
+/* cudaLocksSemaphoreSpin.cu:6-23, cudaLocksSemaphoreEBO.cu:4-21 */
+int cudaSemaphoreCreateSpin(unsigned int* const handle, const int semaphoreNumber, const unsigned int count,
+                            const int NUM_SM);
+int cudaSemaphoreCreateEBO(unsigned int* const handle, const int semaphoreNumber, const unsigned int count,
+                           const int NUM_SM);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HS_H_ */

@@ -1,0 +1,372 @@
+// hs_device.cuh -- sm_103a synchronization primitives for the HeteroSync hot path.
+//
+// Every primitive here is block-collective in the same sense as the reference's
+// device API (all threads of the CTA call it; thread 0 performs the atomics), but
+// it is built on scoped PTX (ld.acquire / st.release / atom / red at .gpu or
+// .cluster scope) instead of volatile accesses plus __threadfence, it polls with a
+// single lane, broadcasts with one bar.red (__syncthreads_or) instead of one
+// __syncthreads per failed poll, and every wait is bounded: a wait that exceeds
+// HsEnv::timeout_ns, or that sees another CTA's error in HsEnv::status, gives up,
+// records HS_DEV_TIMEOUT and the wait site, and returns false so the kernel can
+// exit cleanly (no __trap, no assert, no unbounded spin).
+//
+// Reference algorithms restated here (heterosync, cuda/syncPrims/uvm/):
+//   spin mutex            cudaLocksMutexSpin.cu:13-95
+//   EBO mutex             cudaLocksMutexEBO.cu:13-133
+//   fetch-and-add mutex   cudaLocksMutexFA.cu:13-133
+//   sleep (ring) mutex    cudaLocksMutexSleep.cu:20-199
+//   spin/EBO semaphore    cudaLocksSemaphoreSpin.cu:25-405, cudaLocksSemaphoreEBO.cu:23-457
+//   atomic tree barrier   cudaLocksBarrierAtomic.cu:6-172
+//   lock-free barrier     cudaLocksBarrierFast.cu:10-330
+// The reference-signature wrappers (same names and parameters as those files)
+// are in hs_device_ref.cuh.
+#pragma once
+#include <cstdint>
+
+namespace hs {
+
+// ---------------------------------------------------------------------------
+// Status words shared by all CTAs of one instance.
+//   status[0] : error bits (nonzero means "abort": every waiter gives up)
+//   status[1] : site code of the first failing wait
+// ---------------------------------------------------------------------------
+enum : unsigned {
+  HS_DEV_TIMEOUT = 1u,   // a bounded wait ran out
+  HS_DEV_BADARG  = 2u,   // a kernel saw arguments it cannot honour
+  HS_DEV_TORN    = 4u,   // a semaphore reader saw a torn snapshot (inc mode check)
+};
+
+// Wait-site codes (status[1]); one per spin loop so a timeout names its loop.
+enum : unsigned {
+  HS_SITE_SPIN_LOCK = 1, HS_SITE_EBO_LOCK = 2, HS_SITE_FA_LOCK = 3, HS_SITE_SLEEP_LOCK = 4,
+  HS_SITE_SEM_WAIT = 5, HS_SITE_BAR_LOCAL = 6, HS_SITE_BAR_GLOBAL = 7, HS_SITE_BAR_SCAN = 8,
+  HS_SITE_BAR_GO = 9, HS_SITE_BATCH = 10, HS_SITE_SERVE = 11, HS_SITE_RELAXED = 12,
+  HS_SITE_UTS = 13, HS_SITE_EXCH = 14,
+};
+
+struct HsEnv {
+  unsigned* status;                 // 2 words, see above
+  unsigned long long timeout_ns;    // per-wait limit
+};
+
+// Padding: one lock word per 128-byte L2 line.
+constexpr int kLineWords = 32;
+
+// ---------------------------------------------------------------------------
+// Scoped memory operations (generic addressing: global or distributed shared).
+// ---------------------------------------------------------------------------
+enum Scope { GPU = 0, CLUSTER = 1, CTA = 2 };
+
+template <int S> __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  if constexpr (S == CLUSTER) asm volatile("ld.acquire.cluster.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  else if constexpr (S == CTA) asm volatile("ld.acquire.cta.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  else asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+template <int S> __device__ __forceinline__ unsigned ld_relaxed(const unsigned* p) {
+  unsigned v;
+  if constexpr (S == CLUSTER) asm volatile("ld.relaxed.cluster.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  else if constexpr (S == CTA) asm volatile("ld.relaxed.cta.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  else asm volatile("ld.relaxed.gpu.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+template <int S> __device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
+  if constexpr (S == CLUSTER) asm volatile("st.release.cluster.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+  else if constexpr (S == CTA) asm volatile("st.release.cta.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+  else asm volatile("st.release.gpu.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+template <int S> __device__ __forceinline__ void st_relaxed(unsigned* p, unsigned v) {
+  if constexpr (S == CLUSTER) asm volatile("st.relaxed.cluster.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+  else if constexpr (S == CTA) asm volatile("st.relaxed.cta.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+  else asm volatile("st.relaxed.gpu.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+// atom.inc: old = *p; *p = (old >= lim) ? 0 : old + 1   (same wrap rule as atomicInc)
+template <int S> __device__ __forceinline__ unsigned atom_inc_relaxed(unsigned* p, unsigned lim) {
+  unsigned o;
+  if constexpr (S == CLUSTER) asm volatile("atom.relaxed.cluster.inc.u32 %0, [%1], %2;" : "=r"(o) : "l"(p), "r"(lim) : "memory");
+  else asm volatile("atom.relaxed.gpu.inc.u32 %0, [%1], %2;" : "=r"(o) : "l"(p), "r"(lim) : "memory");
+  return o;
+}
+template <int S> __device__ __forceinline__ void red_release_inc(unsigned* p, unsigned lim) {
+  if constexpr (S == CLUSTER) asm volatile("red.release.cluster.inc.u32 [%0], %1;" :: "l"(p), "r"(lim) : "memory");
+  else asm volatile("red.release.gpu.inc.u32 [%0], %1;" :: "l"(p), "r"(lim) : "memory");
+}
+template <int S> __device__ __forceinline__ void red_release_add(unsigned* p, unsigned v) {
+  if constexpr (S == CLUSTER) asm volatile("red.release.cluster.add.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+  else asm volatile("red.release.gpu.add.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+template <int S> __device__ __forceinline__ unsigned atom_add_acqrel(unsigned* p, unsigned v) {
+  unsigned o;
+  if constexpr (S == CLUSTER) asm volatile("atom.acq_rel.cluster.add.u32 %0, [%1], %2;" : "=r"(o) : "l"(p), "r"(v) : "memory");
+  else asm volatile("atom.acq_rel.gpu.add.u32 %0, [%1], %2;" : "=r"(o) : "l"(p), "r"(v) : "memory");
+  return o;
+}
+template <int S> __device__ __forceinline__ unsigned atom_cas_acquire(unsigned* p, unsigned cmp, unsigned val) {
+  unsigned o;
+  if constexpr (S == CLUSTER) asm volatile("atom.acquire.cluster.cas.b32 %0, [%1], %2, %3;" : "=r"(o) : "l"(p), "r"(cmp), "r"(val) : "memory");
+  else asm volatile("atom.acquire.gpu.cas.b32 %0, [%1], %2, %3;" : "=r"(o) : "l"(p), "r"(cmp), "r"(val) : "memory");
+  return o;
+}
+template <int S> __device__ __forceinline__ unsigned atom_or_relaxed(unsigned* p, unsigned v) {
+  unsigned o;
+  if constexpr (S == CLUSTER) asm volatile("atom.relaxed.cluster.or.b32 %0, [%1], %2;" : "=r"(o) : "l"(p), "r"(v) : "memory");
+  else asm volatile("atom.relaxed.gpu.or.b32 %0, [%1], %2;" : "=r"(o) : "l"(p), "r"(v) : "memory");
+  return o;
+}
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void sleep_ns(unsigned ns) {
+  if (ns) __nanosleep(ns);
+}
+
+// Record a failure (first site wins) and raise the abort bit for everyone.
+__device__ __forceinline__ void fail(const HsEnv& env, unsigned bits, unsigned site) {
+  atomicOr(env.status, bits);
+  atomicCAS(env.status + 1, 0u, site);
+}
+
+// Bounded wait executed by ONE thread.  cond() is re-evaluated after backoff();
+// every 16 polls the status word and the timer are checked.  Returns true once
+// cond() holds, false on timeout or when another CTA has already failed.
+template <class Cond, class Backoff>
+__device__ __forceinline__ bool wait_until(Cond cond, Backoff backoff, const HsEnv& env, unsigned site) {
+  if (cond()) return true;
+  const unsigned long long t0 = globaltimer();
+  unsigned polls = 0;
+  for (;;) {
+    backoff();
+    if (cond()) return true;
+    if ((++polls & 15u) == 0u) {
+      if (ld_relaxed<GPU>(env.status) != 0u) return false;
+      if (globaltimer() - t0 > env.timeout_ns) { fail(env, HS_DEV_TIMEOUT, site); return false; }
+    }
+  }
+}
+
+__device__ __forceinline__ bool is_master() {
+  return threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0;
+}
+
+// Capped exponential sequence used by the reference EBO primitives:
+// b -> ((b << 1) + 1) & (cap - 1)   (1, 3, 7, ..., cap-1; cap a power of two)
+__device__ __forceinline__ unsigned ebo_next(unsigned b, unsigned cap) {
+  return ((b << 1) + 1u) & (cap - 1u);
+}
+
+// ---------------------------------------------------------------------------
+// Mutexes.  lock_* returns (to every thread) whether the lock was taken.
+// unlock_* must follow a successful lock_* and is called by all threads.
+// ---------------------------------------------------------------------------
+
+// Spin (test-and-test-and-set) mutex: CAS 0->1 with acquire, release store 0.
+template <int S>
+__device__ __forceinline__ bool spin_lock(unsigned* lock, const HsEnv& env) {
+  int ok = 0;  // non-masters contribute 0, so the bar.red OR is the master's result
+  if (is_master()) {
+    ok = wait_until([&] { return ld_relaxed<S>(lock) == 0u && atom_cas_acquire<S>(lock, 0u, 1u) == 0u; },
+                    [] {}, env, HS_SITE_SPIN_LOCK);
+  }
+  return __syncthreads_or(ok) != 0;
+}
+template <int S>
+__device__ __forceinline__ void spin_unlock(unsigned* lock) {
+  __syncthreads();  // every thread's critical-section stores precede the release
+  if (is_master()) st_release<S>(lock, 0u);
+}
+
+// Exponential-backoff mutex: as spin, sleeping b ns after each failed try,
+// b following the reference's capped sequence starting at bmin (cap bmax, pow2).
+template <int S>
+__device__ __forceinline__ bool ebo_lock(unsigned* lock, unsigned bmin, unsigned bmax, const HsEnv& env) {
+  int ok = 0;  // non-masters contribute 0, so the bar.red OR is the master's result
+  if (is_master()) {
+    unsigned b = bmin;
+    ok = wait_until([&] { return ld_relaxed<S>(lock) == 0u && atom_cas_acquire<S>(lock, 0u, 1u) == 0u; },
+                    [&] { sleep_ns(b); b = ebo_next(b, bmax); }, env, HS_SITE_EBO_LOCK);
+  }
+  return __syncthreads_or(ok) != 0;
+}
+
+// Fetch-and-add (ticket) mutex.  ticket/turn wrap at `wrap` like atomicInc.
+// The wait sleeps in proportion to the number of tickets ahead (unit ns per
+// position, capped at bmax); unit == 0 spins.
+template <int S>
+__device__ __forceinline__ bool ticket_lock(unsigned* ticket, unsigned* turn, unsigned wrap,
+                                            unsigned unit, unsigned bmax, const HsEnv& env) {
+  int ok = 0;  // non-masters contribute 0, so the bar.red OR is the master's result
+  if (is_master()) {
+    const unsigned my = atom_inc_relaxed<S>(ticket, wrap);
+    unsigned cur = 0;
+    ok = wait_until([&] { cur = ld_acquire<S>(turn); return cur == my; },
+                    [&] {
+                      if (unit) {
+                        unsigned ahead = (my >= cur) ? (my - cur) : (my + wrap + 1u - cur);
+                        unsigned ns = ahead > 1u ? (ahead - 1u) * unit : 0u;
+                        sleep_ns(ns < bmax ? ns : bmax);
+                      }
+                    },
+                    env, HS_SITE_FA_LOCK);
+  }
+  return __syncthreads_or(ok) != 0;
+}
+template <int S>
+__device__ __forceinline__ void ticket_unlock(unsigned* turn, unsigned wrap) {
+  __syncthreads();
+  if (is_master()) red_release_inc<S>(turn, wrap);
+}
+
+// Ring-buffer (array queue) "sleep" mutex.  A waiter takes slot
+// atomicInc(tail, max_slot) and waits for ring[slot] == 1; unlock writes -1 to
+// its slot and 1 to the next (wrapping after max_slot).  Slots are `stride`
+// words apart.  The slot is returned to every thread through shared memory.
+template <int S>
+__device__ __forceinline__ int queue_lock(unsigned* tail, unsigned* ring, unsigned stride,
+                                          unsigned max_slot, unsigned spin_ns, const HsEnv& env,
+                                          int* s_slot) {
+  int ok = 0;  // non-masters contribute 0, so the bar.red OR is the master's result
+  if (is_master()) {
+    const unsigned slot = atom_inc_relaxed<S>(tail, max_slot);
+    *s_slot = (int)slot;
+    unsigned* mine = ring + (size_t)slot * stride;
+    ok = wait_until([&] { return ld_acquire<S>(mine) == 1u; }, [&] { sleep_ns(spin_ns); }, env,
+                    HS_SITE_SLEEP_LOCK);
+  }
+  if (!__syncthreads_or(ok)) return -1;
+  return *s_slot;
+}
+template <int S>
+__device__ __forceinline__ void queue_unlock(unsigned* ring, unsigned stride, unsigned max_slot, unsigned slot) {
+  __syncthreads();
+  if (is_master()) {
+    const unsigned next = (slot >= max_slot) ? 0u : slot + 1u;
+    st_relaxed<S>(ring + (size_t)slot * stride, 0xFFFFFFFFu);
+    st_release<S>(ring + (size_t)next * stride, 1u);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Reader/writer semaphore on ONE packed word:
+//   bits 0..30 : count (starts at N+1 == maxc), bit 31 : writer-waiting flag.
+// Admission rules are the reference's (cudaLocksSemaphoreSpin.cu:70-127):
+//   writer needs count == maxc, then count -= maxc and clears writer-waiting;
+//   a refused writer sets writer-waiting;
+//   reader needs writer-waiting == 0 and count > 1, then count -= 1.
+// Post: writer count += maxc, reader count += 1 -- a single red.release.
+// Backoff policy (EBO variants): writers exponential, readers +5 ns linear
+// (reader_linear == true) or exponential (Local variants).
+// ---------------------------------------------------------------------------
+constexpr unsigned kSemWW = 0x80000000u;
+constexpr unsigned kSemCnt = 0x7FFFFFFFu;
+
+template <int S>
+__device__ __forceinline__ bool sem_try_once(unsigned* st, bool writer, unsigned maxc) {
+  const unsigned s = ld_relaxed<S>(st);
+  if (writer) {
+    if ((s & kSemCnt) == maxc) return atom_cas_acquire<S>(st, s, 0u) == s;
+    if (!(s & kSemWW)) atom_or_relaxed<S>(st, kSemWW);
+    return false;
+  }
+  if (!(s & kSemWW) && (s & kSemCnt) > 1u) return atom_cas_acquire<S>(st, s, s - 1u) == s;
+  return false;
+}
+
+template <int S>
+__device__ __forceinline__ bool sem_wait(unsigned* st, bool writer, unsigned maxc, bool ebo, bool reader_linear,
+                                         unsigned bmin, unsigned bmax, const HsEnv& env) {
+  int ok = 0;  // non-masters contribute 0, so the bar.red OR is the master's result
+  if (is_master()) {
+    unsigned b = bmin;
+    ok = wait_until([&] { return sem_try_once<S>(st, writer, maxc); },
+                    [&] {
+                      if (ebo) {
+                        sleep_ns(b);
+                        if (writer || !reader_linear) b = ebo_next(b, bmax);
+                        else b = (b + 5u < bmax) ? b + 5u : bmax;
+                      }
+                    },
+                    env, HS_SITE_SEM_WAIT);
+  }
+  return __syncthreads_or(ok) != 0;
+}
+template <int S>
+__device__ __forceinline__ void sem_post(unsigned* st, bool writer, unsigned maxc) {
+  __syncthreads();
+  if (is_master()) red_release_add<S>(st, writer ? maxc : 1u);
+}
+
+// ---------------------------------------------------------------------------
+// Barriers.  All state is generation-valued and monotonic, so nothing is reset
+// between episodes or launches (the reference's two-counter "facsimile sense
+// reversal", cudaLocksBarrierAtomic.cu:67-81, and its in/out flag resets,
+// cudaLocksBarrierFast.cu:109-161, are replaced by one generation word).
+// ---------------------------------------------------------------------------
+
+// Counter barrier among n arrivals (one thread each).  The last arriver resets
+// the counter and publishes gen+1.  Returns 1 if this thread was the last.
+// `gen` is the caller's copy of the generation for this episode.
+template <int S, class OnLast>
+__device__ __forceinline__ int counter_barrier(unsigned* count, unsigned* genw, unsigned n, unsigned gen,
+                                               unsigned poll_ns, const HsEnv& env, unsigned site,
+                                               OnLast on_last, bool* ok) {
+  const unsigned old = atom_add_acqrel<S>(count, 1u);
+  if (old == n - 1u) {
+    st_relaxed<S>(count, 0u);
+    *ok = on_last();
+    st_release<S>(genw, gen + 1u);
+    return 1;
+  }
+  *ok = wait_until([&] { return ld_acquire<S>(genw) != gen; }, [&] { sleep_ns(poll_ns); }, env, site);
+  return 0;
+}
+
+// Flag wait: all n flags (dense, generation-valued) must reach `target`.
+// Executed by every thread of the CTA (strided scan, like the reference's main
+// TB, cudaLocksBarrierFast.cu:26-61); returns the CTA-wide result.
+template <int S>
+__device__ __forceinline__ bool scan_flags(const unsigned* flags, unsigned n, unsigned target, unsigned poll_ns,
+                                           const HsEnv& env, unsigned site) {
+  int ok = 1;
+  for (unsigned i = threadIdx.x; i < n && ok; i += blockDim.x) {
+    ok = wait_until([&] { return (int)(ld_acquire<S>(flags + i) - target) >= 0; }, [&] { sleep_ns(poll_ns); },
+                    env, site);
+  }
+  return __syncthreads_and(ok) != 0;
+}
+
+// Hardware cluster barrier (all threads of all CTAs in the cluster).
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+
+__device__ __forceinline__ unsigned cluster_ctarank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ unsigned cluster_id_x() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ unsigned cluster_nctarank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
+
+// Map a local shared-memory address to the same address in CTA `rank` of the
+// cluster (distributed shared memory), as a generic pointer.
+template <class T>
+__device__ __forceinline__ T* map_shared_rank(T* p, unsigned rank) {
+  T* r;
+  asm volatile("mapa.u64 %0, %1, %2;" : "=l"(r) : "l"(p), "r"(rank));
+  return r;
+}
+
+}  // namespace hs

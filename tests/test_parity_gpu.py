@@ -1,0 +1,115 @@
+"""GPU parity: every SyncPrims primitive, through the C ABI, against the oracle
+(the reference golden restated in C), bit-exact.
+
+Sizes keep the number of copy shifts per region below numLdSt, so the
+reference-mode result pins the exact number of critical sections (the
+reference golden alone converges after numLdSt shifts).  NUM_SM is overridden
+to small values so that few TBs still form multi-TB logical-SM groups.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ALL_PRIMS = [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15,
+             20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30, 31]
+
+# (threads, numLdSt, numTBs, iters, repeats, nsm): even group sizes
+CASES = [
+    (32, 40, 8, 2, 2, 4),     # 2 TBs per logical SM, multi-pass shift (40 > 32 lines)
+    (256, 10, 6, 1, 1, 3),    # BASELINE thread count
+    (64, 25, 5, 2, 1, 8),     # fewer TBs than SMs
+    (16, 12, 12, 1, 1, 4),    # 3 TBs per logical SM, half-warp TBs
+]
+
+
+def _init(n, seed):
+    rng = np.random.default_rng(seed)
+    return rng.integers(0, 2**32, size=n, dtype=np.uint64).astype(np.uint32)
+
+
+@pytest.mark.parametrize("prim", ALL_PRIMS)
+@pytest.mark.parametrize("mode", ["ref", "inc"])
+def test_parity_host_storage(hs, oracle, prim, mode):
+    for ci, (T, L, G, iters, reps, nsm) in enumerate(CASES):
+        cfg = hs.RunConfig(prim=prim, num_ldst=L, num_tbs=G, num_iters=iters, threads=T, repeats=reps,
+                           mode=mode, nsm=nsm, timeout_ns=5_000_000_000)
+        n = hs.storage_words(cfg)
+        init = _init(n, prim * 100 + ci)
+        st = init.copy()
+        res = hs.run(cfg, st)
+        want = oracle.golden(prim, T, L, G, iters, reps, nsm, mode == "inc", init)
+        assert res.status == 0 and res.launches == reps
+        bad = np.flatnonzero(st != want)
+        assert bad.size == 0, "prim %d mode %s case %d: %d words differ, first %s" % (
+            prim, mode, ci, bad.size, bad[:8])
+
+
+@pytest.mark.parametrize("prim", [4, 5, 6, 7, 20, 21, 22, 23])
+def test_slice_mode(hs, oracle, prim):
+    """BASELINE workload: uint32[numTBs*numLdSt] seeded in [0,1000), +1 per critical section."""
+    for (T, L, G, iters, reps, nsm) in [(256, 10, 8, 100, 1, 0), (64, 7, 24, 20, 2, 4), (32, 33, 17, 9, 1, 5)]:
+        cfg = hs.RunConfig(prim=prim, num_ldst=L, num_tbs=G, num_iters=iters, threads=T, repeats=reps,
+                           mode="slice", nsm=nsm)
+        n = hs.storage_words(cfg)
+        rng = np.random.default_rng(20260101)
+        init = (rng.integers(0, 2**63, size=n, dtype=np.uint64) % 1000).astype(np.uint32)
+        st = init.copy()
+        hs.run(cfg, st)
+        nsm_eff = nsm or hs.device_info()["nsm"]
+        want = oracle.slice_replay(prim >= 20, L, G, iters, reps, nsm_eff, init)
+        assert np.array_equal(st, want)
+
+
+def test_device_storage_torch(hs, oracle):
+    torch = pytest.importorskip("torch")
+    cfg = hs.RunConfig(prim="faMutex", num_ldst=30, num_tbs=8, num_iters=3, threads=256, repeats=1, mode="ref")
+    n = hs.storage_words(cfg)
+    init = _init(n, 7)
+    t = torch.from_numpy(init.view(np.int32).copy()).cuda()
+    res = hs.run(cfg, t)
+    torch.cuda.synchronize()
+    got = t.cpu().numpy().view(np.uint32)
+    want = oracle.golden(7, 256, 30, 8, 3, 1, hs.device_info()["nsm"], False, init)
+    assert np.array_equal(got, want)
+    assert res.ops == 8 * 3
+
+
+@pytest.mark.parametrize("prim", [0, 2])
+def test_barrier_timeout_is_reported(hs, prim):
+    """A TB that never arrives makes the others' bounded waits run out: the run
+    returns HS_ETIMEDOUT, nothing hangs, and the context stays usable."""
+    cfg = hs.RunConfig(prim=prim, num_ldst=4, num_tbs=16, num_iters=4, threads=64, repeats=1, mode="inc",
+                       nsm=8, timeout_ns=20_000_000, skip_tb=5)
+    st = np.zeros(hs.storage_words(cfg), dtype=np.uint32)
+    res = hs.run(cfg, st, check=False)
+    assert res.status == 2  # HS_ETIMEDOUT
+    assert res.dev_error_bits & 1
+    assert res.dev_error_site in (6, 7, 8, 9)
+    ok = hs.RunConfig(prim=prim, num_ldst=4, num_tbs=16, num_iters=4, threads=64, repeats=1, mode="inc", nsm=8)
+    st = np.zeros(hs.storage_words(ok), dtype=np.uint32)
+    assert hs.run(ok, st).status == 0
+
+
+def test_barrier_co_residency_rejected(hs):
+    nsm = hs.device_info()["nsm"]
+    cfg = hs.RunConfig(prim="atomicTreeBarrUniq", num_ldst=1, num_tbs=nsm * 64, num_iters=1, threads=1024,
+                       repeats=1)
+    st = np.zeros(hs.storage_words(cfg), dtype=np.uint32)
+    res = hs.run(cfg, st, check=False)
+    assert res.status == 3  # HS_ENORES, rejected before launch
+    assert res.launches == 0
+
+
+def test_uneven_barrier_groups_complete(hs, oracle):
+    """numTBs not a multiple of NUM_SM: the reference kernels deadlock here
+    (README.txt:80); these barriers count each group's real members."""
+    for prim in (0, 2):
+        cfg = hs.RunConfig(prim=prim, num_ldst=20, num_tbs=11, num_iters=3, threads=32, repeats=2, mode="inc",
+                           nsm=4, timeout_ns=2_000_000_000)
+        n = hs.storage_words(cfg)
+        init = _init(n, 11)
+        st = init.copy()
+        hs.run(cfg, st)
+        want = oracle.golden(prim, 32, 20, 11, 3, 2, 4, True, init)
+        assert np.array_equal(st, want)
