@@ -65,3 +65,56 @@ def slice_replay(uniq: bool, L: int, num_tbs: int, iters: int, repeats: int, nsm
     if rc:
         raise ValueError("oracle slice replay rejected the configuration")
     return s
+
+
+# ---------------------------------------------------------------------------
+# The reference's own kernels (oracle/_ref/*.cubin, built by build_ref.sh from
+# the unmodified reference sources) run through oracle/ref_runner.cpp.
+# ---------------------------------------------------------------------------
+REF_DIR = os.path.join(HERE, "_ref")
+REF_LIB = os.path.join(HERE, "_build", "libhsref.so")
+_ref = None
+
+
+def ref_module(threads: int) -> str:
+    return os.path.join(REF_DIR, "syncprims_t%d_sm100.cubin" % threads)
+
+
+def ref_available(threads: int = 32) -> bool:
+    return os.path.exists(ref_module(threads)) and os.path.exists(REF_LIB)
+
+
+def _reflib() -> ctypes.CDLL:
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_LIB):
+            build()
+        L = ctypes.CDLL(REF_LIB)
+        L.hs_ref_last_error.restype = ctypes.c_char_p
+        L.hs_ref_run.argtypes = [ctypes.c_char_p] + [ctypes.c_int] * 7 + [ctypes.c_void_p, ctypes.c_long,
+                                                                           ctypes.POINTER(ctypes.c_float)]
+        _ref = L
+    return _ref
+
+
+def ref_device():
+    n, t = ctypes.c_int(), ctypes.c_int()
+    rc = _reflib().hs_ref_device(ctypes.byref(n), ctypes.byref(t))
+    if rc:
+        raise RuntimeError(_reflib().hs_ref_last_error().decode())
+    return n.value, t.value
+
+
+def ref_run(prim: int, T: int, L: int, num_tbs: int, iters: int, repeats: int, init: np.ndarray,
+            sync_each: bool = True):
+    """Run the reference kernel; returns (final storage uint32, elapsed ms over all repeats).
+    Raises RuntimeError when the runner refuses (a launch that would deadlock) or fails."""
+    if not os.path.exists(ref_module(T)):
+        raise FileNotFoundError("no reference module for %d threads per TB" % T)
+    s = np.array(init, dtype=np.uint32, copy=True)
+    ms = ctypes.c_float()
+    rc = _reflib().hs_ref_run(ref_module(T).encode(), T, prim, L, num_tbs, iters, repeats, int(sync_each),
+                              s.ctypes.data, s.size, ctypes.byref(ms))
+    if rc:
+        raise RuntimeError("reference run refused/failed (%d): %s" % (rc, _reflib().hs_ref_last_error().decode()))
+    return s, float(ms.value)

@@ -1,0 +1,58 @@
+"""Generate tests/golden/ref_syncprims.json: final storage of the reference's
+OWN SyncPrims kernels (oracle/_ref, built from the unmodified reference sources)
+for small configurations, recorded as SHA-256 digests plus leading words.
+
+Run on a GPU machine:  python tests/golden/make_ref_fixtures.py OUT.json
+The CPU test test_ref_fixtures_cpu.py recomputes the oracle golden for each
+entry and compares digests, pinning the oracle to the reference itself.
+Initial storage is the reference's storage[i] = i (as float).
+"""
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+import oracle  # noqa: E402
+
+# (prim, threads, numLdSt, numTBs as "k*NSM+c" multiplier/offset, iters, repeats)
+CASES = [
+    (7, 32, 25, (0, 2), 1, 10), (4, 32, 25, (0, 2), 1, 10), (5, 32, 25, (0, 2), 1, 10),
+    (6, 32, 25, (0, 2), 1, 10), (7, 256, 30, (0, 3), 1, 10), (4, 256, 12, (0, 1), 1, 10),
+    (20, 32, 25, (1, 8), 1, 10), (21, 32, 25, (1, 8), 1, 10), (22, 32, 25, (1, 8), 1, 10),
+    (23, 32, 25, (1, 8), 1, 10), (23, 256, 25, (1, 8), 1, 10),
+    (8, 32, 25, (2, 0), 1, 1), (9, 32, 25, (2, 0), 1, 1), (10, 32, 25, (1, 0), 2, 1),
+    (11, 32, 25, (0, 5), 1, 2), (12, 32, 25, (2, 0), 1, 1), (13, 32, 25, (2, 0), 1, 1),
+    (14, 32, 25, (1, 0), 2, 1), (15, 32, 25, (0, 5), 1, 2), (10, 256, 25, (2, 0), 1, 1),
+    (24, 32, 25, (2, 0), 1, 10), (25, 32, 25, (2, 0), 1, 10), (26, 32, 25, (1, 0), 2, 5),
+    (27, 32, 25, (0, 7), 1, 10), (28, 32, 25, (2, 0), 1, 10), (29, 32, 25, (2, 0), 1, 10),
+    (30, 32, 25, (1, 0), 2, 5), (31, 32, 25, (0, 7), 1, 10), (26, 256, 25, (2, 0), 1, 10),
+    (0, 32, 25, (1, 0), 2, 10), (1, 32, 45, (2, 0), 2, 10), (2, 32, 25, (1, 0), 2, 10),
+    (3, 32, 45, (2, 0), 2, 10), (0, 256, 25, (2, 0), 2, 10), (1, 256, 45, (4, 0), 2, 10),
+    (2, 256, 25, (4, 0), 2, 10), (3, 256, 45, (2, 0), 2, 10), (1, 32, 25, (0, 100), 2, 10),
+]
+
+
+def main(out):
+    nsm, _ = oracle.ref_device()
+    entries = []
+    for prim, T, L, (mul, off), iters, reps in CASES:
+        G = mul * nsm + off
+        n = oracle.storage_words(prim, T, L, G, nsm)
+        init = np.arange(n, dtype=np.float32).view(np.uint32)
+        final, ms = oracle.ref_run(prim, T, L, G, iters, reps, init)
+        entries.append({"prim": prim, "threads": T, "num_ldst": L, "num_tbs": G, "iters": iters,
+                        "repeats": reps, "nsm": nsm, "words": int(n),
+                        "sha256": hashlib.sha256(final.tobytes()).hexdigest(),
+                        "head": [int(x) for x in final[:48]], "ref_ms": ms})
+        print(prim, T, L, G, iters, reps, "ok %.3f ms" % ms, flush=True)
+    with open(out, "w") as f:
+        json.dump({"generator": "tests/golden/make_ref_fixtures.py", "init": "storage[i] = (float)i",
+                   "entries": entries}, f, indent=1)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(os.path.dirname(__file__), "ref_syncprims.json"))
