@@ -163,6 +163,15 @@ extern "C" int hs_ref_run(const char* cubin, int T, int prim, int L, int numTBs,
   if ((r = hs_ref_device(&NUM_SM, &max_tpb))) return r;
   const int MAX_BLOCKS = (max_tpb / T) * NUM_SM;  // main.cu:1192-1195
   if (numTBs > MAX_BLOCKS) { g_msg = "numTBs > MAX_BLOCKS"; return 1; }
+  if (rp->kind == 3) {
+    // The reference's per-SM semaphore kernels (kernelSpinLockSemaphoreUniq /
+    // kernelEBOSemaphoreUniq) did not finish on GB300 (spinSemUniq1, 304 TBs x 32
+    // threads: killed after 900 s).  cudaSemaphore*TryWaitLocal reads the count
+    // with a plain load after only __threadfence_block(), so a CTA can keep
+    // reading a stale copy and retry forever.  Never launched again.
+    g_msg = "reference Uniq semaphore kernels livelock on this GPU (stale per-SM count reads); not run";
+    return 3;
+  }
   if (rp->kind == 0) {
     if (!(numTBs <= NUM_SM || numTBs % NUM_SM == 0)) {
       g_msg = "barrier numTBs neither <= NUM_SM nor a multiple of it: the reference kernel would deadlock";
