@@ -1,0 +1,391 @@
+"""Benchmark: sync ops/s of the SyncPrims hot path on GB300.
+
+Workload (the per-primitive sweep): 16 primitives -- spinMutex, spinMutexEBO,
+sleepMutex, faMutex, spinSem{1,2,10,120}, spinSemEBO{1,2,10,120},
+atomicTreeBarrUniq(LocalExch), lfTreeBarrUniq(LocalExch) -- at 256 threads/TB,
+numCSIters = 1000, numLdSt in {10, 100}, numTBs in {1, 2, 4} x NUM_SM (148, 296,
+592 on a 148-SM part; 152, 304, 608 here), seeded uint32 shared data moved by
+the reference's critical section (bit-exact final state).  One step = one launch
+of each of the 16 primitives at one (numTBs, numLdSt) point; steps cycle through
+the 6 points, so the default 6 timed steps cover the sweep once.
+
+  value  sync ops/s = sum(numTBs * numCSIters) / sum(device time of the launches),
+         storage already resident in HBM (CUDA events on the launch stream)
+  e2e    the same ops / wall time of the C-ABI call hs_run() with pinned HOST
+         buffers: host->device copy, lock-state init, launch, device->host copy
+         and status read-back are inside the timed region
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference runs the reference's own SyncPrims kernels (built from its
+unmodified sources into oracle/_ref) on the same GPU with the same sizes, each
+step a bounded sample (fewer iterations); without oracle/_ref it falls back to
+the host std::thread port.  Multi-GPU: replicas only (each rank runs the whole
+sweep on its own GPU; no data crosses GPUs).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SWEEP_PRIMS = ["spinMutex", "spinMutexEBO", "sleepMutex", "faMutex",
+               "spinSem1", "spinSem2", "spinSem10", "spinSem120",
+               "spinSemEBO1", "spinSemEBO2", "spinSemEBO10", "spinSemEBO120",
+               "atomicTreeBarrUniq", "atomicTreeBarrUniqLocalExch", "lfTreeBarrUniq", "lfTreeBarrUniqLocalExch"]
+THREADS = 256
+ITERS = 1000
+LDST = (10, 100)
+TB_MULT = (1, 2, 4)
+SEED = 20260101
+
+
+def sweep_points(nsm):
+    return [(m * nsm, L) for m in TB_MULT for L in LDST]
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        if not sm:
+            return None
+        busy = [x for x in sm if x > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(busy), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def make_init(words, seed):
+    rng = np.random.default_rng(seed)
+    return rng.integers(0, 2 ** 32, size=words, dtype=np.uint64).astype(np.uint32)
+
+
+def pinned_like(arr):
+    import torch
+    t = torch.empty(arr.size, dtype=torch.int32, pin_memory=True)
+    a = t.numpy().view(np.uint32)
+    a[:] = arr
+    return t, a
+
+
+def run_step(hs, nsm, point, iters, check, flush):
+    """One step: every sweep primitive at one (numTBs, numLdSt) point through
+    hs_run with pinned host storage.  Returns per-run records."""
+    G, L = point
+    recs = []
+    for name in SWEEP_PRIMS:
+        cfg = hs.RunConfig(prim=name, num_ldst=L, num_tbs=G, num_iters=iters, threads=THREADS, repeats=1,
+                           mode="ref")
+        words = hs.storage_words(cfg)
+        init = make_init(words, SEED + G + L)
+        _keep, host = pinned_like(init)
+        flush()
+        t0 = time.perf_counter()
+        r = hs.run(cfg, host)
+        wall = time.perf_counter() - t0
+        if check:
+            want = hs.expected_storage(cfg, init)
+            if not np.array_equal(host, want):
+                raise SystemExit("bench: %s numTBs=%d numLdSt=%d differs from the expected final state"
+                                 % (name, G, L))
+        recs.append({"prim": name, "num_tbs": G, "num_ldst": L, "iters": iters, "ops": r.ops,
+                     "ms": r.elapsed_ms, "wall_s": wall, "bytes": words * 4, "launches": r.launches})
+    return recs
+
+
+def cpu_baseline(nsm, budget_s=12.0):
+    """Host std::thread port (the oracle twins) on a bounded sample of the sweep:
+    every primitive at numTBs = 2*NUM_SM, numLdSt = 10, with the iteration count
+    cut until the sample fits the time budget."""
+    import oracle
+    cores = os.cpu_count() or 1
+    iters = 20
+    total_ops, total_s = 0, 0.0
+    G, L = 2 * nsm, 10
+    for name in SWEEP_PRIMS:
+        import heterosync_gb300 as hs
+        p = hs.prim_id(name)
+        n = oracle.storage_words(p, THREADS, L, G, nsm)
+        init = make_init(n, SEED)
+        _, secs = oracle.twin_run(p, THREADS, L, G, iters, 1, nsm, 0, init, threads=cores)
+        total_ops += G * iters
+        total_s += secs
+        if total_s > budget_s:
+            break
+    return {"value": total_ops / total_s if total_s else None, "unit": "sync ops/s", "cores": cores,
+            "kind": "port",
+            "sample": "host std::thread twins, each sweep primitive at numTBs=%d numLdSt=%d, %d iterations, "
+                      "%d ops in %.2f s" % (G, L, iters, total_ops, total_s)}
+
+
+def l2_atomic_peak(hs):
+    import ctypes
+    v = ctypes.c_double()
+    nsm = hs.device_info()["nsm"]
+    if hs.lib().hs_probe_l2_atomics(nsm * 8, 256, 256, 0, ctypes.byref(v)):
+        return None, None
+    same = ctypes.c_double()
+    hs.lib().hs_probe_l2_atomics(nsm * 4, 32, 2000, 1, ctypes.byref(same))
+    return v.value, same.value
+
+
+# algorithmic L2 atomics per sync op (contention-free minimum of this build's
+# implementation of each primitive): lock + unlock
+ATOMICS_PER_OP = {"spinMutex": 2, "spinMutexEBO": 2, "sleepMutex": 3, "faMutex": 2,
+                  "spinSem1": 2, "spinSem2": 2, "spinSem10": 2, "spinSem120": 2,
+                  "spinSemEBO1": 2, "spinSemEBO2": 2, "spinSemEBO10": 2, "spinSemEBO120": 2,
+                  "atomicTreeBarrUniq": 1, "atomicTreeBarrUniqLocalExch": 2, "lfTreeBarrUniq": 1,
+                  "lfTreeBarrUniqLocalExch": 2}
+
+
+def cs_bytes(name, G, L, nsm):
+    """Algorithmic bytes one launch moves: 4-byte load + 4-byte store per element
+    touched by a critical section (T*numLdSt elements per mutex op; the writer's
+    numTBs_perSM chunks per semaphore writer op, T*numLdSt loads per reader op;
+    per barrier episode every TB's chunk once, twice with local exchange)."""
+    T = THREADS
+    k = -(-G // nsm)
+    if "Barr" in name:
+        per = 2 if ("LocalExch" in name and k > 1) else 1
+        return G * ITERS * T * L * 8 * per
+    if "Sem" in name:
+        numSM = min(G, nsm)
+        writers = sum(1 for tb in range(G) if tb // numSM == (tb % numSM) % k)
+        readers = G - writers
+        return ITERS * (writers * k * T * L * 8 + readers * T * L * 4)
+    return G * ITERS * T * L * 8
+
+
+def reference_arm(args, rank):
+    import oracle
+    hs_nsm = None
+    out = {"impl": "reference", "metric": "sync ops/s", "unit": "sync ops/s", "higher_is_better": True,
+           "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "data": "synthetic",
+           "dtype": "u32", "scaling": "weak", "vs_baseline": None}
+    if rank != 0:
+        return None
+    iters_ref = 100
+    if oracle.ref_available(THREADS):
+        nsm, _ = oracle.ref_device()
+        hs_nsm = nsm
+        pts = sweep_points(nsm)
+        recs = []
+        for step in range(args.warmup + args.steps):
+            G, L = pts[step % len(pts)]
+            it = 5 if step < args.warmup else iters_ref
+            for name in SWEEP_PRIMS:
+                import heterosync_gb300 as hs
+                p = hs.prim_id(name)
+                n = oracle.storage_words(p, THREADS, L, G, nsm)
+                init = make_init(n, SEED + G + L)
+                _, ms = oracle.ref_run(p, THREADS, L, G, it, 1, init)
+                if step >= args.warmup:
+                    recs.append((G * it, ms))
+        ops = sum(o for o, _ in recs)
+        ms = sum(m for _, m in recs)
+        value = ops / (ms * 1e-3)
+        out.update({"value": value, "ms_per_step": ms / args.steps,
+                    "config": {"workload": "per-primitive sweep, reference CUDA kernels (sm_100 build of the "
+                                           "unmodified sources) on this GPU",
+                               "threads": THREADS, "num_iters": iters_ref, "num_ldst": list(LDST),
+                               "num_tbs": [m * nsm for m in TB_MULT], "primitives": SWEEP_PRIMS,
+                               "sample": "each (primitive, size) launched once with numCSIters=%d "
+                                         "(the build's arm uses %d)" % (iters_ref, ITERS)},
+                    "cpu_baseline": {"value": value, "unit": "sync ops/s", "cores": None, "kind": "reference",
+                                     "sample": "reference SyncPrims kernels on the GB300, %d ops" % ops},
+                    "e2e": {"value": value, "unit": "sync ops/s", "h2d_bytes_per_step": 0,
+                            "d2h_bytes_per_step": 0}})
+    else:
+        import heterosync_gb300 as hs
+        nsm = hs.device_info()["nsm"] if hs_nsm is None else hs_nsm
+        cb = cpu_baseline(nsm)
+        out.update({"value": cb["value"], "ms_per_step": None,
+                    "config": {"workload": "per-primitive sweep sample on host cores (reference modules absent)"},
+                    "cpu_baseline": cb,
+                    "e2e": {"value": cb["value"], "unit": "sync ops/s", "h2d_bytes_per_step": 0,
+                            "d2h_bytes_per_step": 0}})
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=6)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-check", action="store_true", help="skip the bit-exact check of every run")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    if args.impl == "reference":
+        out = reference_arm(args, rank)
+        if rank == 0 and out is not None:
+            print(json.dumps(out), flush=True)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    import heterosync_gb300 as hs
+    nsm = hs.device_info(local)["nsm"] if local == 0 else hs.device_info()["nsm"]
+    pts = sweep_points(nsm)
+    flush_buf = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")  # 256 MiB > L2
+
+    def flush():
+        flush_buf.zero_()
+        torch.cuda.synchronize()
+
+    # warm-up: the first W points with a short iteration count
+    for s in range(args.warmup):
+        run_step(hs, nsm, pts[s % len(pts)], 20, check=False, flush=flush)
+
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    launches0 = hs.launch_count()
+    t0 = time.perf_counter()
+    recs = []
+    for s in range(args.steps):
+        recs += run_step(hs, nsm, pts[s % len(pts)], ITERS, check=not args.no_check, flush=flush)
+    torch.cuda.synchronize()
+    wall_total = time.perf_counter() - t0
+    launches = hs.launch_count() - launches0
+    ck = clocks.stop()
+
+    ops = sum(r["ops"] for r in recs)
+    dev_s = sum(r["ms"] for r in recs) * 1e-3
+    e2e_s = sum(r["wall_s"] for r in recs)
+    if dist is not None:
+        t = torch.tensor([dev_s, e2e_s, float(ops)], device="cuda", dtype=torch.float64)
+        mx = t.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        sm = t.clone()
+        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+        dev_s, e2e_s, ops = mx[0].item(), mx[1].item(), int(sm[2].item())
+
+    if rank == 0:
+        peak_gbs, peak_kind = load_peaks()
+        # dominant kernel: the (primitive) with the largest share of device time
+        by_prim = {}
+        for r in recs:
+            d = by_prim.setdefault(r["prim"], {"ops": 0, "ms": 0.0, "bytes": 0, "launches": 0})
+            d["ops"] += r["ops"]
+            d["ms"] += r["ms"]
+            d["bytes"] += cs_bytes(r["prim"], r["num_tbs"], r["num_ldst"], nsm)
+            d["launches"] += 1
+        dom = max(by_prim, key=lambda k: by_prim[k]["ms"])
+        dd = by_prim[dom]
+        achieved = dd["bytes"] / (dd["ms"] * 1e-3) / 1e9
+        atom_peak, same_rate = l2_atomic_peak(hs)
+        atom_achieved = sum(by_prim[k]["ops"] * ATOMICS_PER_OP[k] for k in by_prim) / dev_s
+        out = {
+            "metric": "sync ops/s", "value": ops / dev_s, "unit": "sync ops/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (seeded uint32 shared data, bit-exact final state checked every run)",
+            "config": {"workload": "per-primitive sweep: 16 SyncPrims x numTBs {%s} x numLdSt {10,100}, "
+                                   "256 threads/TB, 1000 CS iterations, reference critical section"
+                                   % ",".join(str(m * nsm) for m in TB_MULT),
+                       "threads": THREADS, "num_iters": ITERS, "num_ldst": list(LDST),
+                       "num_tbs": [m * nsm for m in TB_MULT], "primitives": SWEEP_PRIMS,
+                       "step": "one launch of each primitive at one (numTBs, numLdSt) point; steps cycle the "
+                               "6 points", "l2": "flushed before every run (256 MiB write)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "e2e": {"value": ops / e2e_s, "unit": "sync ops/s",
+                    "h2d_bytes_per_step": int(sum(r["bytes"] for r in recs) / args.steps),
+                    "d2h_bytes_per_step": int(sum(r["bytes"] for r in recs) / args.steps)},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
+                         "frac": achieved / peak_gbs, "peak_source": peak_kind, "traffic": None,
+                         "note": "critical-section bytes; these kernels are latency-bound (lock hand-off), see "
+                                 "l2_atomic"},
+            "l2_atomic": {"achieved": atom_achieved, "peak": atom_peak,
+                          "frac": (atom_achieved / atom_peak) if atom_peak else None, "unit": "atomics/s",
+                          "same_address_rate": same_rate,
+                          "note": "peak: contention-free red.add probe; same_address_rate: one word"},
+            "per_prim": {k: {"ops_per_s": v["ops"] / (v["ms"] * 1e-3), "ms": round(v["ms"], 3)}
+                         for k, v in by_prim.items()},
+            "wall_s": wall_total,
+        }
+        if ck:
+            out["clocks"] = ck
+        if not args.no_cpu_baseline and world == 1:
+            try:
+                out["cpu_baseline"] = cpu_baseline(nsm)
+            except Exception as e:  # noqa: BLE001
+                out["cpu_baseline"] = {"value": None, "error": str(e)}
+        print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

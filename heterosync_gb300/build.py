@@ -32,6 +32,7 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", ARCH, "-Xcompiler", "-fPIC", "-I
 CU_SOURCES = [
     "hs_syncprims.cu",
     "hs_api.cu",
+    "hs_probe.cu",
 ]
 # command-line programs: (output name, source)
 PROGRAMS = [

@@ -117,6 +117,13 @@ int hs_run(hs_ctx* ctx, const hs_run_config* cfg, void* storage, int storage_on_
  * the reference's golden replay, main.cu:1633-1788).  Host arrays. */
 int hs_expected_storage(const hs_run_config* cfg, int nsm, const uint32_t* init, uint32_t* expected, size_t words);
 
+/* ---- roofline probes --------------------------------------------------------- */
+/* Aggregate L2 atomic rate: blocks x threads threads each issue `iters`
+ * red.add to their own 128-byte-spaced word (same_address = 0: contention-free
+ * peak), or one lane per block to a single word (same_address = 1: the rate one
+ * contended lock word sustains).  Result in atomics per second. */
+int hs_probe_l2_atomics(int blocks, int threads, int iters, int same_address, double* atomics_per_s);
+
 /* ---- the reference's host API (cuda/syncPrims/uvm/cudaLocks.h:4-26) ----------- */
 /* Same field order as cudaLockData_t (cudaLocks.h:4-16). */
 typedef struct hs_lock_data {

@@ -118,3 +118,20 @@ def ref_run(prim: int, T: int, L: int, num_tbs: int, iters: int, repeats: int, i
     if rc:
         raise RuntimeError("reference run refused/failed (%d): %s" % (rc, _reflib().hs_ref_last_error().decode()))
     return s, float(ms.value)
+
+
+def twin_run(prim: int, T: int, L: int, num_tbs: int, iters: int, repeats: int, nsm: int, mode: int,
+             init: np.ndarray, threads: int = 0):
+    """Host std::thread run of the same algorithm; returns (final storage, seconds)."""
+    L_ = lib()
+    if not hasattr(L_, "_twin_ready"):
+        L_.hs_twin_run.argtypes = [ctypes.c_int] * 8 + [ctypes.c_void_p, ctypes.c_long, ctypes.c_int,
+                                                         ctypes.POINTER(ctypes.c_double)]
+        L_._twin_ready = True
+    s = np.array(init, dtype=np.uint32, copy=True)
+    secs = ctypes.c_double()
+    rc = L_.hs_twin_run(prim, T, L, num_tbs, iters, repeats, nsm, mode, s.ctypes.data, s.size, threads,
+                        ctypes.byref(secs))
+    if rc:
+        raise ValueError("twin rejected the configuration")
+    return s, float(secs.value)
