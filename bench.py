@@ -220,7 +220,14 @@ def reference_arm(args, rank):
            "dtype": "u32", "scaling": "weak", "vs_baseline": None}
     if rank != 0:
         return None
-    iters_ref = 100
+    # bounded sample: the reference's semaphores take ~0.2 ms per op under contention
+    def iters_ref_for(name):
+        if "Barr" in name:
+            return 200
+        if "Sem" in name:
+            return 3
+        return 30
+    iters_ref = "per family: barriers 200, mutexes 30, semaphores 3"
     if oracle.ref_available(THREADS):
         nsm, _ = oracle.ref_device()
         hs_nsm = nsm
@@ -228,8 +235,8 @@ def reference_arm(args, rank):
         recs = []
         for step in range(args.warmup + args.steps):
             G, L = pts[step % len(pts)]
-            it = 5 if step < args.warmup else iters_ref
             for name in SWEEP_PRIMS:
+                it = 1 if step < args.warmup else iters_ref_for(name)
                 import heterosync_gb300 as hs
                 p = hs.prim_id(name)
                 n = oracle.storage_words(p, THREADS, L, G, nsm)
@@ -245,7 +252,7 @@ def reference_arm(args, rank):
                                            "unmodified sources) on this GPU",
                                "threads": THREADS, "num_iters": iters_ref, "num_ldst": list(LDST),
                                "num_tbs": [m * nsm for m in TB_MULT], "primitives": SWEEP_PRIMS,
-                               "sample": "each (primitive, size) launched once with numCSIters=%d "
+                               "sample": "each (primitive, size) launched once with numCSIters %s "
                                          "(the build's arm uses %d)" % (iters_ref, ITERS)},
                     "cpu_baseline": {"value": value, "unit": "sync ops/s", "cores": None, "kind": "reference",
                                      "sample": "reference SyncPrims kernels on the GB300, %d ops" % ops},

@@ -14,7 +14,7 @@
 
 namespace hs {
 using KernelFn = void (*)(RunDesc);
-KernelFn syncprim_kernel(int prim, int mode, int threads);
+KernelFn syncprim_kernel(int prim, int mode, int threads, int num_ldst);
 cudaError_t launch_ring_init(unsigned* ring, unsigned slots_per_group, unsigned groups, cudaStream_t st);
 cudaError_t launch_fill_lines(unsigned* base, size_t n, size_t stride, unsigned value, cudaStream_t st);
 }  // namespace hs
@@ -448,7 +448,7 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c, void* storage, int on
   hs_storage_words(c, nsm, &words);
   const size_t bytes = words * 4;
 
-  KernelFn fn = syncprim_kernel(c->prim, c->mode, c->threads);
+  KernelFn fn = syncprim_kernel(c->prim, c->mode, c->threads, c->num_ldst);
   if (!fn) { g_err = "no kernel for this primitive/mode"; return r->status = HS_EINVAL; }
   if (is_barrier(c->prim)) {
     int per_sm = 0;

@@ -117,14 +117,16 @@ __device__ __forceinline__ void cs_read(const unsigned* chunk, int T, int L, uns
   if ((threadIdx.x & 31) == 0 && acc == 0x9E3779B9u) *sink_slot = acc;  // practically never taken
 }
 
-// Threads per CTA above 512 get a smaller register budget per thread.
-template <bool BIG> struct Bounds { static constexpr int kThreads = BIG ? 1024 : 512; static constexpr int kVec = BIG ? 4 : 8; };
+// Vector depth V = 16-byte vectors each thread keeps in flight per pass.  The
+// launch bound follows from it: V 4 -> 1024 threads, 8 -> 512, 26 -> 256 (a
+// 256-thread TB then moves numLdSt <= 104 lines of its chunk in one pass).
+template <int V> struct Bounds { static constexpr int kThreads = V <= 4 ? 1024 : (V <= 8 ? 512 : 256); };
 
-template <int MODE, bool BIG = false>
+template <int MODE, int V>
 __device__ __forceinline__ void cs_chunk(const RunDesc& d, int chunk) {
   unsigned* c = d.data + (size_t)chunk * chunk_words(d.T, d.L);
-  if constexpr (MODE == M_REF) cs_ref_shift<Bounds<BIG>::kVec>(c, d.T, d.L);
-  else cs_inc<Bounds<BIG>::kVec>(c, d.T, d.L);
+  if constexpr (MODE == M_REF) cs_ref_shift<V>(c, d.T, d.L);
+  else cs_inc<V>(c, d.T, d.L);
 }
 
 __device__ __forceinline__ unsigned* group_line(const RunDesc& d, int g, int k) {
@@ -135,8 +137,8 @@ __device__ __forceinline__ unsigned* group_line(const RunDesc& d, int g, int k) 
 // Mutex kernels: main.cu:317-529.  Global variants: one lock, every TB works on
 // chunk 0.  Uniq variants: lock and chunk per logical SM (blockIdx % NUM_SM).
 // ---------------------------------------------------------------------------
-template <int KIND, bool UNIQ, int MODE, bool BIG>
-__global__ void __launch_bounds__(Bounds<BIG>::kThreads) k_mutex(RunDesc d) {
+template <int KIND, bool UNIQ, int MODE, int V>
+__global__ void __launch_bounds__(Bounds<V>::kThreads) k_mutex(RunDesc d) {
   __shared__ int s_slot;
   const int b = blockIdx.x;
   const int g = UNIQ ? (b % d.nsm) : 0;
@@ -164,7 +166,7 @@ __global__ void __launch_bounds__(Bounds<BIG>::kThreads) k_mutex(RunDesc d) {
     if (!ok) break;
 
     if constexpr (MODE == M_SLICE) cs_slice(d.data, g + ((r + j) % m) * G, d.L);
-    else cs_chunk<MODE, BIG>(d, g);
+    else cs_chunk<MODE, V>(d, g);
 
     if constexpr (KIND == MK_SPIN || KIND == MK_EBO) spin_unlock<GPU>(w0);
     else if constexpr (KIND == MK_FA) ticket_unlock<GPU>(w1, wrap);
@@ -176,8 +178,8 @@ __global__ void __launch_bounds__(Bounds<BIG>::kThreads) k_mutex(RunDesc d) {
 // Semaphore kernels: main.cu:533-836.  One writer TB per logical SM
 // (perSM_blockID == smID % numTBs_perSM); the rest are readers.
 // ---------------------------------------------------------------------------
-template <bool EBO, bool UNIQ, int MODE, bool BIG>
-__global__ void __launch_bounds__(Bounds<BIG>::kThreads) k_sem(RunDesc d) {
+template <bool EBO, bool UNIQ, int MODE, int V>
+__global__ void __launch_bounds__(Bounds<V>::kThreads) k_sem(RunDesc d) {
   const int b = blockIdx.x;
   const int Gd = d.num_tbs;
   const int numSM = Gd < d.nsm ? Gd : d.nsm;
@@ -195,11 +197,11 @@ __global__ void __launch_bounds__(Bounds<BIG>::kThreads) k_sem(RunDesc d) {
       if constexpr (UNIQ) {
         int cur = b;
         for (int j = 0; j < k; ++j) {
-          cs_chunk<MODE, BIG>(d, cur);
+          cs_chunk<MODE, V>(d, cur);
           cur = (cur + numSM) % Gd;
         }
       } else {
-        for (int j = 0; j < k; ++j) cs_chunk<MODE, BIG>(d, j);
+        for (int j = 0; j < k; ++j) cs_chunk<MODE, V>(d, j);
       }
     } else {
       cs_read(d.data + (size_t)rchunk * chunk_words(d.T, d.L), d.T, d.L, d.sink + b);
@@ -323,8 +325,8 @@ __device__ __forceinline__ bool tree_barrier(const RunDesc& d, int g, int r, int
   }
 }
 
-template <bool LF, bool EXCH, int MODE, bool BIG>
-__global__ void __launch_bounds__(Bounds<BIG>::kThreads) k_barrier(RunDesc d) {
+template <bool LF, bool EXCH, int MODE, int V>
+__global__ void __launch_bounds__(Bounds<V>::kThreads) k_barrier(RunDesc d) {
   const int b = blockIdx.x;
   const int Gd = d.num_tbs;
   const int nb = Gd < d.nsm ? Gd : d.nsm;
@@ -346,12 +348,12 @@ __global__ void __launch_bounds__(Bounds<BIG>::kThreads) k_barrier(RunDesc d) {
 
   int cur = b;
   for (int i = 0; i < d.iters; ++i) {
-    cs_chunk<MODE, BIG>(d, cur);
+    cs_chunk<MODE, V>(d, cur);
     if (b == d.skip_tb) return;  // fault injection: this TB never arrives
     if (EXCH && kmax > 1) {
       if (!local_only_barrier<LF>(d, g, r, m, s, env)) return;
       cur = (cur + nb) % Gd;
-      cs_chunk<MODE, BIG>(d, cur);
+      cs_chunk<MODE, V>(d, cur);
     }
     if (!tree_barrier<LF>(d, g, r, m, nb, s, env)) return;
     cur = (cur + 1) % Gd;
@@ -373,42 +375,53 @@ __global__ void k_ring_init(unsigned* ring, unsigned slots_per_group, unsigned g
 // ---------------------------------------------------------------------------
 using KernelFn = void (*)(RunDesc);
 
-template <int MODE, bool BIG>
+template <int MODE, int V>
 static KernelFn pick(int prim) {
   if constexpr (MODE != M_SLICE) {
-    switch (prim) {
-      case P_ATOMIC_TREE: return k_barrier<false, false, MODE, BIG>;
-      case P_ATOMIC_TREE_EXCH: return k_barrier<false, true, MODE, BIG>;
-      case P_LF_TREE: return k_barrier<true, false, MODE, BIG>;
-      case P_LF_TREE_EXCH: return k_barrier<true, true, MODE, BIG>;
-      default: break;
+    if constexpr (V <= 8) {  // barriers need all TBs co-resident: small register budget only
+      switch (prim) {
+        case P_ATOMIC_TREE: return k_barrier<false, false, MODE, V>;
+        case P_ATOMIC_TREE_EXCH: return k_barrier<false, true, MODE, V>;
+        case P_LF_TREE: return k_barrier<true, false, MODE, V>;
+        case P_LF_TREE_EXCH: return k_barrier<true, true, MODE, V>;
+        default: break;
+      }
     }
-    if (prim >= P_SPIN_SEM1 && prim <= P_SPIN_SEM120) return k_sem<false, false, MODE, BIG>;
-    if (prim >= P_EBO_SEM1 && prim <= P_EBO_SEM120) return k_sem<true, false, MODE, BIG>;
-    if (prim >= P_SPIN_SEM_UNIQ1 && prim <= P_SPIN_SEM_UNIQ120) return k_sem<false, true, MODE, BIG>;
-    if (prim >= P_EBO_SEM_UNIQ1 && prim <= P_EBO_SEM_UNIQ120) return k_sem<true, true, MODE, BIG>;
+    if (prim >= P_SPIN_SEM1 && prim <= P_SPIN_SEM120) return k_sem<false, false, MODE, V>;
+    if (prim >= P_EBO_SEM1 && prim <= P_EBO_SEM120) return k_sem<true, false, MODE, V>;
+    if (prim >= P_SPIN_SEM_UNIQ1 && prim <= P_SPIN_SEM_UNIQ120) return k_sem<false, true, MODE, V>;
+    if (prim >= P_EBO_SEM_UNIQ1 && prim <= P_EBO_SEM_UNIQ120) return k_sem<true, true, MODE, V>;
   }
   switch (prim) {
-    case P_SPIN_MUTEX: return k_mutex<MK_SPIN, false, MODE, BIG>;
-    case P_EBO_MUTEX: return k_mutex<MK_EBO, false, MODE, BIG>;
-    case P_SLEEP_MUTEX: return k_mutex<MK_SLEEP, false, MODE, BIG>;
-    case P_FA_MUTEX: return k_mutex<MK_FA, false, MODE, BIG>;
-    case P_SPIN_MUTEX_UNIQ: return k_mutex<MK_SPIN, true, MODE, BIG>;
-    case P_EBO_MUTEX_UNIQ: return k_mutex<MK_EBO, true, MODE, BIG>;
-    case P_SLEEP_MUTEX_UNIQ: return k_mutex<MK_SLEEP, true, MODE, BIG>;
-    case P_FA_MUTEX_UNIQ: return k_mutex<MK_FA, true, MODE, BIG>;
+    case P_SPIN_MUTEX: return k_mutex<MK_SPIN, false, MODE, V>;
+    case P_EBO_MUTEX: return k_mutex<MK_EBO, false, MODE, V>;
+    case P_SLEEP_MUTEX: return k_mutex<MK_SLEEP, false, MODE, V>;
+    case P_FA_MUTEX: return k_mutex<MK_FA, false, MODE, V>;
+    case P_SPIN_MUTEX_UNIQ: return k_mutex<MK_SPIN, true, MODE, V>;
+    case P_EBO_MUTEX_UNIQ: return k_mutex<MK_EBO, true, MODE, V>;
+    case P_SLEEP_MUTEX_UNIQ: return k_mutex<MK_SLEEP, true, MODE, V>;
+    case P_FA_MUTEX_UNIQ: return k_mutex<MK_FA, true, MODE, V>;
     default: return nullptr;
   }
 }
 
-KernelFn syncprim_kernel(int prim, int mode, int threads) {
-  const bool big = threads > 512;
+template <int V>
+static KernelFn pick_v(int prim, int mode) {
   switch (mode) {
-    case M_REF: return big ? pick<M_REF, true>(prim) : pick<M_REF, false>(prim);
-    case M_INC: return big ? pick<M_INC, true>(prim) : pick<M_INC, false>(prim);
-    case M_SLICE: return big ? pick<M_SLICE, true>(prim) : pick<M_SLICE, false>(prim);
+    case M_REF: return pick<M_REF, V>(prim);
+    case M_INC: return pick<M_INC, V>(prim);
+    case M_SLICE: return pick<M_SLICE, V>(prim);
     default: return nullptr;
   }
+}
+
+// Deepest vector variant that the thread count (and, for barriers, the
+// co-residency the caller checks) allows.
+KernelFn syncprim_kernel(int prim, int mode, int threads, int num_ldst) {
+  const bool barrier = prim >= P_ATOMIC_TREE && prim <= P_LF_TREE_EXCH;
+  if (threads > 512) return pick_v<4>(prim, mode);
+  if (threads > 256 || barrier || num_ldst <= 32) return pick_v<8>(prim, mode);
+  return pick_v<26>(prim, mode);
 }
 
 __global__ void k_fill_lines(unsigned* base, size_t n, size_t stride, unsigned value) {
