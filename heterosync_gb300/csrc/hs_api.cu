@@ -392,7 +392,7 @@ int hs_prepare_run(hs_ctx* ctx, const hs_run_config* c, int nsm, void* dev_stora
   d->bo_max = c->backoff_max_ns ? c->backoff_max_ns : 1024u;
   d->bo_unit = c->backoff_unit_ns;
   d->ring_max = (unsigned)c->num_tbs;
-  d->timeout_ns = c->timeout_ns ? c->timeout_ns : 2000000000ull;
+  d->timeout_ns = c->timeout_ns ? c->timeout_ns : 10000000000ull;
   d->skip_tb = c->skip_tb;
   d->cluster = 1;
   d->l_glob = lay.l_glob;

@@ -62,7 +62,7 @@ typedef struct hs_run_config {
   unsigned backoff_min_ns;   /* EBO start (reference 1) */
   unsigned backoff_max_ns;   /* EBO cap, power of two (reference MAX_BACKOFF = 1024) */
   unsigned backoff_unit_ns;  /* ticket-lock per-position sleep / poll sleep (0 = spin) */
-  unsigned long long timeout_ns; /* per-wait limit, 0 = 2 s */
+  unsigned long long timeout_ns; /* per-wait limit without observed progress, 0 = 10 s */
   int skip_tb;          /* fault injection for barriers: this TB never arrives (-1 = none) */
   int flags;            /* HS_RUN_* */
 } hs_run_config;

@@ -134,19 +134,40 @@ __device__ __forceinline__ void fail(const HsEnv& env, unsigned bits, unsigned s
 // Bounded wait executed by ONE thread.  cond() is re-evaluated after backoff();
 // every 16 polls the status word and the timer are checked.  Returns true once
 // cond() holds, false on timeout or when another CTA has already failed.
-template <class Cond, class Backoff>
-__device__ __forceinline__ bool wait_until(Cond cond, Backoff backoff, const HsEnv& env, unsigned site) {
+//
+// progress() names a word other waiters' progress changes (a ticket lock's turn,
+// a semaphore's state): whenever its value moves, the timer restarts, so a
+// waiter that is legitimately behind many others (a reader held off by a long
+// writer phase) never times out while the system advances; a wait times out
+// only after timeout_ns with no observed progress.
+template <class Cond, class Progress, class Backoff>
+__device__ __forceinline__ bool wait_until_p(Cond cond, Progress progress, Backoff backoff, const HsEnv& env,
+                                             unsigned site) {
   if (cond()) return true;
-  const unsigned long long t0 = globaltimer();
+  unsigned long long t0 = globaltimer();
+  unsigned last = progress();
   unsigned polls = 0;
   for (;;) {
     backoff();
     if (cond()) return true;
     if ((++polls & 15u) == 0u) {
       if (ld_relaxed<GPU>(env.status) != 0u) return false;
-      if (globaltimer() - t0 > env.timeout_ns) { fail(env, HS_DEV_TIMEOUT, site); return false; }
+      const unsigned long long now = globaltimer();
+      const unsigned p = progress();
+      if (p != last) {
+        last = p;
+        t0 = now;
+      } else if (now - t0 > env.timeout_ns) {
+        fail(env, HS_DEV_TIMEOUT, site);
+        return false;
+      }
     }
   }
+}
+
+template <class Cond, class Backoff>
+__device__ __forceinline__ bool wait_until(Cond cond, Backoff backoff, const HsEnv& env, unsigned site) {
+  return wait_until_p(cond, [] { return 0u; }, backoff, env, site);
 }
 
 __device__ __forceinline__ bool is_master() {
@@ -203,7 +224,7 @@ __device__ __forceinline__ bool ticket_lock(unsigned* ticket, unsigned* turn, un
   if (is_master()) {
     const unsigned my = atom_inc_relaxed<S>(ticket, wrap);
     unsigned cur = 0;
-    ok = wait_until([&] { cur = ld_acquire<S>(turn); return cur == my; },
+    ok = wait_until_p([&] { cur = ld_acquire<S>(turn); return cur == my; }, [&] { return cur; },
                     [&] {
                       if (unit) {
                         unsigned ahead = (my >= cur) ? (my - cur) : (my + wrap + 1u - cur);
@@ -234,8 +255,9 @@ __device__ __forceinline__ int queue_lock(unsigned* tail, unsigned* ring, unsign
     const unsigned slot = atom_inc_relaxed<S>(tail, max_slot);
     *s_slot = (int)slot;
     unsigned* mine = ring + (size_t)slot * stride;
-    ok = wait_until([&] { return ld_acquire<S>(mine) == 1u; }, [&] { sleep_ns(spin_ns); }, env,
-                    HS_SITE_SLEEP_LOCK);
+    unsigned* prev = ring + (size_t)(slot == 0u ? max_slot : slot - 1u) * stride;
+    ok = wait_until_p([&] { return ld_acquire<S>(mine) == 1u; }, [&] { return ld_relaxed<S>(prev); },
+                      [&] { sleep_ns(spin_ns); }, env, HS_SITE_SLEEP_LOCK);
   }
   if (!__syncthreads_or(ok)) return -1;
   return *s_slot;
@@ -282,7 +304,7 @@ __device__ __forceinline__ bool sem_wait(unsigned* st, bool writer, unsigned max
   int ok = 0;  // non-masters contribute 0, so the bar.red OR is the master's result
   if (is_master()) {
     unsigned b = bmin;
-    ok = wait_until([&] { return sem_try_once<S>(st, writer, maxc); },
+    ok = wait_until_p([&] { return sem_try_once<S>(st, writer, maxc); }, [&] { return ld_relaxed<S>(st); },
                     [&] {
                       if (ebo) {
                         sleep_ns(b);

@@ -29,7 +29,7 @@
 #define HS_REF_MAX_BACKOFF 1024u  // reference main.cu:7 (MAX_BACKOFF)
 #endif
 #ifndef HS_REF_TIMEOUT_NS
-#define HS_REF_TIMEOUT_NS 2000000000ull
+#define HS_REF_TIMEOUT_NS 10000000000ull
 #endif
 
 typedef unsigned int cudaMutex_t;      // reference cudaLocks.h:18
