@@ -325,8 +325,10 @@ __device__ __forceinline__ bool tree_barrier(const RunDesc& d, int g, int r, int
   }
 }
 
+// Barrier TBs must all be co-resident, so the kernel is held to 64 registers
+// (four 256-thread TBs, 1024 threads, per SM).
 template <bool LF, bool EXCH, int MODE, int V>
-__global__ void __launch_bounds__(Bounds<V>::kThreads) k_barrier(RunDesc d) {
+__global__ void __launch_bounds__(Bounds<V>::kThreads, 1024 / Bounds<V>::kThreads) k_barrier(RunDesc d) {
   const int b = blockIdx.x;
   const int Gd = d.num_tbs;
   const int nb = Gd < d.nsm ? Gd : d.nsm;
@@ -347,13 +349,17 @@ __global__ void __launch_bounds__(Bounds<V>::kThreads) k_barrier(RunDesc d) {
   BarState s = s_init;
 
   int cur = b;
+  const int phases = (EXCH && kmax > 1) ? 2 : 1;
   for (int i = 0; i < d.iters; ++i) {
-    cs_chunk<MODE, V>(d, cur);
-    if (b == d.skip_tb) return;  // fault injection: this TB never arrives
-    if (EXCH && kmax > 1) {
-      if (!local_only_barrier<LF>(d, g, r, m, s, env)) return;
-      cur = (cur + nb) % Gd;
+    // phase 0: own chunk; phase 1 (local exchange): local barrier, then the chunk
+    // numBlocksAtBarr TBs ahead (one call site keeps one inlined copy of the CS)
+    for (int ph = 0; ph < phases; ++ph) {
+      if (ph == 1) {
+        if (!local_only_barrier<LF>(d, g, r, m, s, env)) return;
+        cur = (cur + nb) % Gd;
+      }
       cs_chunk<MODE, V>(d, cur);
+      if (b == d.skip_tb) return;  // fault injection: this TB never arrives
     }
     if (!tree_barrier<LF>(d, g, r, m, nb, s, env)) return;
     cur = (cur + 1) % Gd;
