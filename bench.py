@@ -149,29 +149,31 @@ def run_step(hs, nsm, point, iters, check, flush):
     return recs
 
 
-def cpu_baseline(nsm, budget_s=12.0):
-    """Host std::thread port (the oracle twins) on a bounded sample of the sweep:
-    every primitive at numTBs = 2*NUM_SM, numLdSt = 10, with the iteration count
-    cut until the sample fits the time budget."""
+def cpu_baseline(nsm, budget_s=15.0):
+    """Host std::thread port (the oracle twins) on a bounded sample of the same
+    sweep: every (primitive, numTBs, numLdSt) cell, each with an untimed
+    5-iteration pilot and then a timed run whose iteration count spreads
+    `budget_s` of CPU work evenly over the cells (at most 1000 iterations)."""
     import oracle
+    import heterosync_gb300 as hs
     cores = os.cpu_count() or 1
-    iters = 20
-    total_ops, total_s = 0, 0.0
-    G, L = 2 * nsm, 10
-    for name in SWEEP_PRIMS:
-        import heterosync_gb300 as hs
+    cells = [(name, G, L) for (G, L) in sweep_points(nsm) for name in SWEEP_PRIMS]
+    per_cell = budget_s / len(cells)
+    total_ops, total_s, iters_used = 0, 0.0, []
+    for name, G, L in cells:
         p = hs.prim_id(name)
         n = oracle.storage_words(p, THREADS, L, G, nsm)
         init = make_init(n, SEED)
-        _, secs = oracle.twin_run(p, THREADS, L, G, iters, 1, nsm, 0, init, threads=cores)
-        total_ops += G * iters
+        _, s5 = oracle.twin_run(p, THREADS, L, G, 5, 1, nsm, 0, init, threads=cores)
+        it = int(max(5, min(ITERS, 5 * per_cell / max(s5, 1e-6))))
+        _, secs = oracle.twin_run(p, THREADS, L, G, it, 1, nsm, 0, init, threads=cores)
+        total_ops += G * it
         total_s += secs
-        if total_s > budget_s:
-            break
+        iters_used.append(it)
     return {"value": total_ops / total_s if total_s else None, "unit": "sync ops/s", "cores": cores,
             "kind": "port",
-            "sample": "host std::thread twins, each sweep primitive at numTBs=%d numLdSt=%d, %d iterations, "
-                      "%d ops in %.2f s" % (G, L, iters, total_ops, total_s)}
+            "sample": "host std::thread twins over all %d sweep cells, numCSIters %d-%d per cell (pilot-scaled), "
+                      "%d ops in %.1f s" % (len(cells), min(iters_used), max(iters_used), total_ops, total_s)}
 
 
 def l2_atomic_peak(hs):
@@ -220,30 +222,33 @@ def reference_arm(args, rank):
            "dtype": "u32", "scaling": "weak", "vs_baseline": None}
     if rank != 0:
         return None
-    # bounded sample: the reference's semaphores take ~0.2 ms per op under contention
-    def iters_ref_for(name):
-        if "Barr" in name:
-            return 200
-        if "Sem" in name:
-            return 3
-        return 30
-    iters_ref = "per family: barriers 200, mutexes 30, semaphores 3"
+    # Bounded sample: the reference's semaphores take 0.2 ms or more per op under
+    # contention, so each (primitive, size) gets an untimed 1-iteration pilot and
+    # then one timed launch whose iteration count targets ~0.4 s (at most 1000).
+    target_ms = 400.0
+    iters_ref = "adaptive: 1-iteration pilot, then numCSIters = clamp(400 ms / pilot, 1, 1000)"
     if oracle.ref_available(THREADS):
         nsm, _ = oracle.ref_device()
         hs_nsm = nsm
         pts = sweep_points(nsm)
         recs = []
+        chosen = {}
         for step in range(args.warmup + args.steps):
             G, L = pts[step % len(pts)]
             for name in SWEEP_PRIMS:
-                it = 1 if step < args.warmup else iters_ref_for(name)
                 import heterosync_gb300 as hs
                 p = hs.prim_id(name)
                 n = oracle.storage_words(p, THREADS, L, G, nsm)
                 init = make_init(n, SEED + G + L)
+                key = (name, G, L)
+                if key not in chosen:
+                    _, ms1 = oracle.ref_run(p, THREADS, L, G, 1, 1, init)
+                    chosen[key] = int(max(1, min(1000, target_ms / max(ms1, 1e-3))))
+                if step < args.warmup:
+                    continue
+                it = chosen[key]
                 _, ms = oracle.ref_run(p, THREADS, L, G, it, 1, init)
-                if step >= args.warmup:
-                    recs.append((G * it, ms))
+                recs.append((G * it, ms))
         ops = sum(o for o, _ in recs)
         ms = sum(m for _, m in recs)
         value = ops / (ms * 1e-3)
@@ -380,6 +385,8 @@ def main():
                           "note": "peak: contention-free red.add probe; same_address_rate: one word"},
             "per_prim": {k: {"ops_per_s": v["ops"] / (v["ms"] * 1e-3), "ms": round(v["ms"], 3)}
                          for k, v in by_prim.items()},
+            "per_point_us_per_op": {"%s@%d/%d" % (r["prim"], r["num_tbs"], r["num_ldst"]):
+                                    round(r["ms"] * 1e3 / r["ops"], 3) for r in recs},
             "wall_s": wall_total,
         }
         if ck:
