@@ -222,17 +222,22 @@ def reference_arm(args, rank):
            "dtype": "u32", "scaling": "weak", "vs_baseline": None}
     if rank != 0:
         return None
-    # Bounded sample: the reference's semaphores take 0.2 ms or more per op under
-    # contention, so each (primitive, size) gets an untimed 1-iteration pilot and
-    # then one timed launch whose iteration count targets ~0.4 s (at most 1000).
-    target_ms = 400.0
-    iters_ref = "adaptive: 1-iteration pilot, then numCSIters = clamp(400 ms / pilot, 1, 1000)"
+    # Bounded sample with fixed iteration counts: the reference's semaphores take
+    # 0.1-0.4 ms per op under contention and its EBO readers' backoff grows
+    # without bound (cudaLocksSemaphoreEBO.cu:176), so their run time is not
+    # linear in numCSIters; each semaphore TB does one wait/post.
+    def iters_ref_for(name):
+        if "Barr" in name:
+            return 200
+        if "Sem" in name:
+            return 1
+        return 30
+    iters_ref = "per family: barriers 200, mutexes 30, semaphores 1"
     if oracle.ref_available(THREADS):
         nsm, _ = oracle.ref_device()
         hs_nsm = nsm
         pts = sweep_points(nsm)
         recs = []
-        chosen = {}
         for step in range(args.warmup + args.steps):
             G, L = pts[step % len(pts)]
             for name in SWEEP_PRIMS:
@@ -240,15 +245,10 @@ def reference_arm(args, rank):
                 p = hs.prim_id(name)
                 n = oracle.storage_words(p, THREADS, L, G, nsm)
                 init = make_init(n, SEED + G + L)
-                key = (name, G, L)
-                if key not in chosen:
-                    _, ms1 = oracle.ref_run(p, THREADS, L, G, 1, 1, init)
-                    chosen[key] = int(max(1, min(1000, target_ms / max(ms1, 1e-3))))
-                if step < args.warmup:
-                    continue
-                it = chosen[key]
+                it = 1 if step < args.warmup else iters_ref_for(name)
                 _, ms = oracle.ref_run(p, THREADS, L, G, it, 1, init)
-                recs.append((G * it, ms))
+                if step >= args.warmup:
+                    recs.append((G * it, ms))
         ops = sum(o for o, _ in recs)
         ms = sum(m for _, m in recs)
         value = ops / (ms * 1e-3)
