@@ -167,13 +167,14 @@ def cpu_baseline(nsm, budget_s=15.0):
         _, s5 = oracle.twin_run(p, THREADS, L, G, 5, 1, nsm, 0, init, threads=cores)
         it = int(max(5, min(ITERS, 5 * per_cell / max(s5, 1e-6))))
         _, secs = oracle.twin_run(p, THREADS, L, G, it, 1, nsm, 0, init, threads=cores)
-        total_ops += G * it
-        total_s += secs
+        total_ops += G * ITERS                 # the cell's full-workload ops ...
+        total_s += secs * ITERS / it           # ... at the sampled rate
         iters_used.append(it)
     return {"value": total_ops / total_s if total_s else None, "unit": "sync ops/s", "cores": cores,
             "kind": "port",
-            "sample": "host std::thread twins over all %d sweep cells, numCSIters %d-%d per cell (pilot-scaled), "
-                      "%d ops in %.1f s" % (len(cells), min(iters_used), max(iters_used), total_ops, total_s)}
+            "sample": "host std::thread twins over all %d sweep cells, numCSIters %d-%d per cell (pilot-scaled, "
+                      "~%.0f s of CPU work), each cell's rate projected to its numTBs*1000 ops"
+                      % (len(cells), min(iters_used), max(iters_used), budget_s)}
 
 
 def l2_atomic_peak(hs):
@@ -248,9 +249,12 @@ def reference_arm(args, rank):
                 it = 1 if step < args.warmup else iters_ref_for(name)
                 _, ms = oracle.ref_run(p, THREADS, L, G, it, 1, init)
                 if step >= args.warmup:
-                    recs.append((G * it, ms))
-        ops = sum(o for o, _ in recs)
-        ms = sum(m for _, m in recs)
+                    recs.append((G * it, ms, G * ITERS))
+        # same metric as the build's arm: each cell's measured rate carries the
+        # cell's full-workload ops (numTBs * 1000), and the sweep value is the
+        # full workload's ops over the sum of the projected cell times
+        ops = sum(full for _, _, full in recs)
+        ms = sum(m * full / o for o, m, full in recs)
         value = ops / (ms * 1e-3)
         out.update({"value": value, "ms_per_step": ms / args.steps,
                     "config": {"workload": "per-primitive sweep, reference CUDA kernels (sm_100 build of the "
@@ -260,7 +264,8 @@ def reference_arm(args, rank):
                                "sample": "each (primitive, size) launched once with numCSIters %s "
                                          "(the build's arm uses %d)" % (iters_ref, ITERS)},
                     "cpu_baseline": {"value": value, "unit": "sync ops/s", "cores": None, "kind": "reference",
-                                     "sample": "reference SyncPrims kernels on the GB300, %d ops" % ops},
+                                     "sample": "reference SyncPrims kernels on the GB300, %d sampled ops projected "
+                                               "to the sweep's %d" % (sum(o for o, _, _ in recs), ops)},
                     "e2e": {"value": value, "unit": "sync ops/s", "h2d_bytes_per_step": 0,
                             "d2h_bytes_per_step": 0}})
     else:
