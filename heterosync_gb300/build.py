@@ -33,6 +33,7 @@ CU_SOURCES = [
     "hs_syncprims.cu",
     "hs_api.cu",
     "hs_probe.cu",
+    "hs_noalloc.cu",
 ]
 # command-line programs: (output name, source)
 PROGRAMS = [

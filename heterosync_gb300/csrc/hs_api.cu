@@ -573,3 +573,10 @@ extern "C" int cudaSemaphoreCreateSpin(unsigned int* const h, const int s, const
 extern "C" int cudaSemaphoreCreateEBO(unsigned int* const h, const int s, const unsigned int count, const int nsm) {
   return sem_create(h, s, count, nsm);
 }
+
+// Lock-state layout of a run, for entry points that place the state in memory
+// they do not allocate here.
+int hs_layout_for(const hs_run_config* c, int nsm, hs::Layout* out) {
+  *out = make_layout(c, nsm);
+  return HS_OK;
+}

@@ -117,6 +117,22 @@ int hs_run(hs_ctx* ctx, const hs_run_config* cfg, void* storage, int storage_on_
  * the reference's golden replay, main.cu:1633-1788).  Host arrays. */
 int hs_expected_storage(const hs_run_config* cfg, int nsm, const uint32_t* init, uint32_t* expected, size_t words);
 
+/* ---- runs without device allocation ------------------------------------------ */
+/* No counterpart in the reference.  hs_run() for callers that cannot allocate
+ * device memory -- host frameworks that own all device memory through their own
+ * pool, processes under a device-memory budget fixed at start-up, and
+ * latency-critical loops that cannot afford cudaMalloc's implicit device-wide
+ * synchronisation.  The lock state lives in one fixed device array of
+ * HS_NOALLOC_SCRATCH_BYTES that the library holds on every GPU that loads it;
+ * runs whose state does not fit are rejected with HS_EINVAL.  `storage` must be
+ * device memory.  The first call on a device looks up the array's address:
+ * make it before any stream capture.  All calls share the array, so calls that
+ * overlap on the GPU race; each call clears the state it needs.  elapsed_ms is
+ * host wall time around the launches (no events are created). */
+#define HS_NOALLOC_SCRATCH_BYTES (1u << 20)
+int hs_run_noalloc(const hs_run_config* cfg, void* storage, void* stream, hs_run_result* result);
+const char* hs_noalloc_last_error(void);
+
 /* ---- roofline probes --------------------------------------------------------- */
 /* Aggregate L2 atomic rate: blocks x threads threads each issue `iters`
  * red.add to their own 128-byte-spaced word (same_address = 0: contention-free
