@@ -14,7 +14,8 @@
 
 namespace hs {
 using KernelFn = void (*)(RunDesc);
-KernelFn syncprim_kernel(int prim, int mode, int threads, int num_ldst);
+KernelFn syncprim_plan(int prim, int mode, int threads, int num_ldst, size_t* smem_bytes);
+cudaError_t prepare_smem(KernelFn fn, size_t smem_bytes);
 cudaError_t launch_ring_init(unsigned* ring, unsigned slots_per_group, unsigned groups, cudaStream_t st);
 cudaError_t launch_fill_lines(unsigned* base, size_t n, size_t stride, unsigned value, cudaStream_t st);
 }  // namespace hs
@@ -448,8 +449,10 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c, void* storage, int on
   hs_storage_words(c, nsm, &words);
   const size_t bytes = words * 4;
 
-  KernelFn fn = syncprim_kernel(c->prim, c->mode, c->threads, c->num_ldst);
+  size_t smem = 0;
+  KernelFn fn = syncprim_plan(c->prim, c->mode, c->threads, c->num_ldst, &smem);
   if (!fn) { g_err = "no kernel for this primitive/mode"; return r->status = HS_EINVAL; }
+  HS_CK(prepare_smem(fn, smem));
   if (is_barrier(c->prim)) {
     int per_sm = 0;
     HS_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, c->threads, 0));
@@ -474,7 +477,7 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c, void* storage, int on
   HS_CK(cudaEventRecord(ctx->ev[0], st));
   for (int rep = 0; rep < c->repeats; ++rep) {
     void* args[] = {&d};
-    HS_CK(cudaLaunchKernel((const void*)fn, dim3(c->num_tbs), dim3(c->threads), args, 0, st));
+    HS_CK(cudaLaunchKernel((const void*)fn, dim3(c->num_tbs), dim3(c->threads), args, smem, st));
     r->launches++;
     if (c->flags & HS_RUN_SYNC_EACH) HS_CK(cudaStreamSynchronize(st));
   }

@@ -32,7 +32,8 @@
 
 namespace hs {
 using KernelFn = void (*)(RunDesc);
-KernelFn syncprim_kernel(int prim, int mode, int threads, int num_ldst);
+KernelFn syncprim_plan(int prim, int mode, int threads, int num_ldst, size_t* smem_bytes);
+cudaError_t prepare_smem(KernelFn fn, size_t smem_bytes);
 cudaError_t launch_ring_init(unsigned* ring, unsigned slots_per_group, unsigned groups, cudaStream_t st);
 cudaError_t launch_fill_lines(unsigned* base, size_t n, size_t stride, unsigned value, cudaStream_t st);
 }  // namespace hs
@@ -86,8 +87,10 @@ extern "C" int hs_run_noalloc(const hs_run_config* c, void* storage, void* strea
   size_t words = 0;
   int s = hs_storage_words(c, nsm, &words);
   if (s) { set_err(hs_last_error()); return r->status = s; }
-  KernelFn fn = syncprim_kernel(c->prim, c->mode, c->threads, c->num_ldst);
+  size_t smem = 0;
+  KernelFn fn = syncprim_plan(c->prim, c->mode, c->threads, c->num_ldst, &smem);
   if (!fn) { set_err("no kernel for this primitive/mode"); return r->status = HS_EINVAL; }
+  if (prepare_smem(fn, smem) != cudaSuccess) return r->status = HS_ECUDA;
 
   Layout lay;
   hs_layout_for(c, nsm, &lay);
@@ -165,7 +168,7 @@ extern "C" int hs_run_noalloc(const hs_run_config* c, void* storage, void* strea
   }
   for (int rep = 0; rep < c->repeats; ++rep) {
     void* args[] = {&d};
-    if (cudaLaunchKernel((const void*)fn, dim3(c->num_tbs), dim3(c->threads), args, 0, st) != cudaSuccess)
+    if (cudaLaunchKernel((const void*)fn, dim3(c->num_tbs), dim3(c->threads), args, smem, st) != cudaSuccess)
       return r->status = HS_ECUDA;
     r->launches++;
   }

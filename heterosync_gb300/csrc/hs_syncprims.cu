@@ -117,6 +117,130 @@ __device__ __forceinline__ void cs_read(const unsigned* chunk, int T, int L, uns
   if ((threadIdx.x & 31) == 0 && acc == 0x9E3779B9u) *sink_slot = acc;  // practically never taken
 }
 
+// ---------------------------------------------------------------------------
+// TMA path for large chunks (numLdSt > 32, chunk <= kTmaMaxBytes): one
+// cp.async.bulk copies the whole chunk into shared memory (completion counted
+// on an mbarrier), then one bulk store per half-warp region writes lines
+// 0..L-1 back one line up (INC: lines 1..L after +1 in shared memory).  The
+// copy engine keeps the whole chunk in flight, which roughly doubles one SM's
+// throughput on the critical section over vector loads.
+// Ordering: the acquire (generic proxy) is followed by fence.proxy.async before
+// the bulk load; the bulk stores are completed (wait_group 0) and followed by
+// fence.proxy.async before the release.
+// ---------------------------------------------------------------------------
+constexpr unsigned kTmaMaxBytes = 200u * 1024u;
+
+struct TmaCtx {
+  unsigned char* buf;  // dynamic shared memory, chunk bytes
+  unsigned mbar;       // shared address of the mbarrier
+  unsigned phase;
+};
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void tma_init(TmaCtx& t, unsigned long long* mbar_storage, unsigned char* dyn) {
+  t.buf = dyn;
+  t.mbar = smem_addr(mbar_storage);
+  t.phase = 0;
+  if (is_master()) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(t.mbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ bool mbar_done(unsigned mbar, unsigned phase) {
+  unsigned done;
+  asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+               : "=r"(done) : "r"(mbar), "r"(phase) : "memory");
+  return done != 0;
+}
+
+// Load a chunk into shared memory; returns the CTA-wide success.
+__device__ __forceinline__ bool tma_load_chunk(const unsigned* chunk, unsigned bytes, TmaCtx& t, const HsEnv& env) {
+  if (is_master()) {
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(t.mbar), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(smem_addr(t.buf)), "l"(chunk), "r"(bytes), "r"(t.mbar) : "memory");
+  }
+  const bool ok = wait_until([&] { return mbar_done(t.mbar, t.phase); }, [] {}, env, HS_SITE_TMA);
+  t.phase ^= 1u;
+  return __syncthreads_and(ok) != 0;
+}
+
+// Store lines [first, first+L) of every region of the staged chunk to lines
+// [1, L] of the chunk in global memory, and complete the writes.
+__device__ __forceinline__ void tma_store_shifted(unsigned* chunk, int T, int L, unsigned first, TmaCtx& t) {
+  if (is_master()) {
+    const int R = T >> 4;
+    const unsigned rb = (unsigned)(16 * (L + 1) * 4);
+    const unsigned sbase = smem_addr(t.buf);
+    for (int h = 0; h < R; ++h) {
+      unsigned char* dst = reinterpret_cast<unsigned char*>(chunk) + (size_t)h * rb + 64u;
+      asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                   :: "l"(dst), "r"(sbase + h * rb + first * 64u), "r"((unsigned)(64 * L)) : "memory");
+    }
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+  }
+}
+
+template <int MODE>
+__device__ __forceinline__ bool cs_chunk_tma(const RunDesc& d, int chunk, TmaCtx& t, const HsEnv& env) {
+  unsigned* c = d.data + (size_t)chunk * chunk_words(d.T, d.L);
+  const unsigned bytes = (unsigned)(d.T * (d.L + 1) * 4);
+  if (!tma_load_chunk(c, bytes, t, env)) return false;
+  if constexpr (MODE == M_REF) {
+    tma_store_shifted(c, d.T, d.L, 0u, t);
+  } else {
+    const int R = d.T >> 4, per_region = d.L * 4, rw4 = (d.L + 1) * 4;
+    uint4* s4 = reinterpret_cast<uint4*>(t.buf);
+    for (int i = threadIdx.x; i < R * per_region; i += d.T) {
+      const int h = i / per_region;
+      uint4& v = s4[h * rw4 + 4 + (i - h * per_region)];
+      v.x += 1u; v.y += 1u; v.z += 1u; v.w += 1u;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic smem writes -> bulk store reads
+    __syncthreads();
+    // lines 1..L of smem go to lines 1..L of global: same offsets, so "shift" from line 1 to line 1
+    if (is_master()) {
+      const unsigned rb = (unsigned)(16 * (d.L + 1) * 4);
+      const unsigned sbase = smem_addr(t.buf);
+      for (int h = 0; h < R; ++h) {
+        unsigned char* dst = reinterpret_cast<unsigned char*>(c) + (size_t)h * rb + 64u;
+        asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                     :: "l"(dst), "r"(sbase + h * rb + 64u), "r"((unsigned)(64 * d.L)) : "memory");
+      }
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+      asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+      asm volatile("fence.proxy.async.global;" ::: "memory");
+    }
+  }
+  return true;
+}
+
+// Semaphore reader on the TMA path: stage the chunk, fold lines 0..L-1.
+__device__ __forceinline__ bool cs_read_tma(const RunDesc& d, int chunk, TmaCtx& t, const HsEnv& env,
+                                            unsigned* sink_slot) {
+  const unsigned* c = d.data + (size_t)chunk * chunk_words(d.T, d.L);
+  if (!tma_load_chunk(c, (unsigned)(d.T * (d.L + 1) * 4), t, env)) return false;
+  const int R = d.T >> 4, per_region = d.L * 4, rw4 = (d.L + 1) * 4;
+  const uint4* s4 = reinterpret_cast<const uint4*>(t.buf);
+  unsigned acc = 0;
+  for (int i = threadIdx.x; i < R * per_region; i += d.T) {
+    const int h = i / per_region;
+    const uint4 v = s4[h * rw4 + (i - h * per_region)];
+    acc += v.x ^ v.y ^ v.z ^ v.w;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
+  if ((threadIdx.x & 31) == 0 && acc == 0x9E3779B9u) *sink_slot = acc;
+  __syncthreads();  // the buffer is reused by the next load
+  return true;
+}
+
 // Vector depth V = 16-byte vectors each thread keeps in flight per pass.  The
 // launch bound follows from it: V 4 -> 1024 threads, 8 -> 512, 26 -> 256 (a
 // 256-thread TB then moves numLdSt <= 104 lines of its chunk in one pass).
@@ -137,9 +261,13 @@ __device__ __forceinline__ unsigned* group_line(const RunDesc& d, int g, int k) 
 // Mutex kernels: main.cu:317-529.  Global variants: one lock, every TB works on
 // chunk 0.  Uniq variants: lock and chunk per logical SM (blockIdx % NUM_SM).
 // ---------------------------------------------------------------------------
-template <int KIND, bool UNIQ, int MODE, int V>
-__global__ void __launch_bounds__(Bounds<V>::kThreads) k_mutex(RunDesc d) {
+template <int KIND, bool UNIQ, int MODE, int V, bool TMA = false>
+__global__ void __launch_bounds__(TMA ? 256 : Bounds<V>::kThreads) k_mutex(RunDesc d) {
   __shared__ int s_slot;
+  __shared__ unsigned long long s_mbar;
+  extern __shared__ __align__(128) unsigned char dyn_smem[];
+  TmaCtx tma;
+  if constexpr (TMA) tma_init(tma, &s_mbar, dyn_smem);
   const int b = blockIdx.x;
   const int g = UNIQ ? (b % d.nsm) : 0;
   unsigned* w0 = group_line(d, g, 0);
@@ -166,11 +294,13 @@ __global__ void __launch_bounds__(Bounds<V>::kThreads) k_mutex(RunDesc d) {
     if (!ok) break;
 
     if constexpr (MODE == M_SLICE) cs_slice(d.data, g + ((r + j) % m) * G, d.L);
+    else if constexpr (TMA) ok = cs_chunk_tma<MODE>(d, g, tma, env);
     else cs_chunk<MODE, V>(d, g);
 
     if constexpr (KIND == MK_SPIN || KIND == MK_EBO) spin_unlock<GPU>(w0);
     else if constexpr (KIND == MK_FA) ticket_unlock<GPU>(w1, wrap);
     else queue_unlock<GPU>(ring, kRingStride, d.ring_max, (unsigned)slot);
+    if (!ok) break;  // a bounded copy wait gave up (status already recorded)
   }
 }
 
@@ -178,8 +308,12 @@ __global__ void __launch_bounds__(Bounds<V>::kThreads) k_mutex(RunDesc d) {
 // Semaphore kernels: main.cu:533-836.  One writer TB per logical SM
 // (perSM_blockID == smID % numTBs_perSM); the rest are readers.
 // ---------------------------------------------------------------------------
-template <bool EBO, bool UNIQ, int MODE, int V>
-__global__ void __launch_bounds__(Bounds<V>::kThreads) k_sem(RunDesc d) {
+template <bool EBO, bool UNIQ, int MODE, int V, bool TMA = false>
+__global__ void __launch_bounds__(TMA ? 256 : Bounds<V>::kThreads) k_sem(RunDesc d) {
+  __shared__ unsigned long long s_mbar;
+  extern __shared__ __align__(128) unsigned char dyn_smem[];
+  TmaCtx tma;
+  if constexpr (TMA) tma_init(tma, &s_mbar, dyn_smem);
   const int b = blockIdx.x;
   const int Gd = d.num_tbs;
   const int numSM = Gd < d.nsm ? Gd : d.nsm;
@@ -193,20 +327,20 @@ __global__ void __launch_bounds__(Bounds<V>::kThreads) k_sem(RunDesc d) {
 
   for (int i = 0; i < d.iters; ++i) {
     if (!sem_wait<GPU>(st, writer, d.sem_max, EBO, !UNIQ, d.bo_min, d.bo_max, env)) break;
+    bool ok = true;
     if (writer) {
-      if constexpr (UNIQ) {
-        int cur = b;
-        for (int j = 0; j < k; ++j) {
-          cs_chunk<MODE, V>(d, cur);
-          cur = (cur + numSM) % Gd;
-        }
-      } else {
-        for (int j = 0; j < k; ++j) cs_chunk<MODE, V>(d, j);
+      int cur = UNIQ ? b : 0;
+      for (int j = 0; j < k && ok; ++j) {
+        if constexpr (TMA) ok = cs_chunk_tma<MODE>(d, cur, tma, env);
+        else cs_chunk<MODE, V>(d, cur);
+        cur = UNIQ ? (cur + numSM) % Gd : cur + 1;
       }
     } else {
-      cs_read(d.data + (size_t)rchunk * chunk_words(d.T, d.L), d.T, d.L, d.sink + b);
+      if constexpr (TMA) ok = cs_read_tma(d, rchunk, tma, env, d.sink + b);
+      else cs_read(d.data + (size_t)rchunk * chunk_words(d.T, d.L), d.T, d.L, d.sink + b);
     }
     sem_post<GPU>(st, writer, d.sem_max);
+    if (!ok) break;
   }
 }
 
@@ -381,10 +515,10 @@ __global__ void k_ring_init(unsigned* ring, unsigned slots_per_group, unsigned g
 // ---------------------------------------------------------------------------
 using KernelFn = void (*)(RunDesc);
 
-template <int MODE, int V>
+template <int MODE, int V, bool TMA>
 static KernelFn pick(int prim) {
   if constexpr (MODE != M_SLICE) {
-    if constexpr (V <= 8) {  // barriers need all TBs co-resident: small register budget only
+    if constexpr (!TMA) {  // barriers need all TBs co-resident: register path only
       switch (prim) {
         case P_ATOMIC_TREE: return k_barrier<false, false, MODE, V>;
         case P_ATOMIC_TREE_EXCH: return k_barrier<false, true, MODE, V>;
@@ -393,41 +527,72 @@ static KernelFn pick(int prim) {
         default: break;
       }
     }
-    if (prim >= P_SPIN_SEM1 && prim <= P_SPIN_SEM120) return k_sem<false, false, MODE, V>;
-    if (prim >= P_EBO_SEM1 && prim <= P_EBO_SEM120) return k_sem<true, false, MODE, V>;
-    if (prim >= P_SPIN_SEM_UNIQ1 && prim <= P_SPIN_SEM_UNIQ120) return k_sem<false, true, MODE, V>;
-    if (prim >= P_EBO_SEM_UNIQ1 && prim <= P_EBO_SEM_UNIQ120) return k_sem<true, true, MODE, V>;
-  }
-  switch (prim) {
-    case P_SPIN_MUTEX: return k_mutex<MK_SPIN, false, MODE, V>;
-    case P_EBO_MUTEX: return k_mutex<MK_EBO, false, MODE, V>;
-    case P_SLEEP_MUTEX: return k_mutex<MK_SLEEP, false, MODE, V>;
-    case P_FA_MUTEX: return k_mutex<MK_FA, false, MODE, V>;
-    case P_SPIN_MUTEX_UNIQ: return k_mutex<MK_SPIN, true, MODE, V>;
-    case P_EBO_MUTEX_UNIQ: return k_mutex<MK_EBO, true, MODE, V>;
-    case P_SLEEP_MUTEX_UNIQ: return k_mutex<MK_SLEEP, true, MODE, V>;
-    case P_FA_MUTEX_UNIQ: return k_mutex<MK_FA, true, MODE, V>;
-    default: return nullptr;
+    if (prim >= P_SPIN_SEM1 && prim <= P_SPIN_SEM120) return k_sem<false, false, MODE, V, TMA>;
+    if (prim >= P_EBO_SEM1 && prim <= P_EBO_SEM120) return k_sem<true, false, MODE, V, TMA>;
+    if (prim >= P_SPIN_SEM_UNIQ1 && prim <= P_SPIN_SEM_UNIQ120) return k_sem<false, true, MODE, V, TMA>;
+    if (prim >= P_EBO_SEM_UNIQ1 && prim <= P_EBO_SEM_UNIQ120) return k_sem<true, true, MODE, V, TMA>;
+    switch (prim) {
+      case P_SPIN_MUTEX: return k_mutex<MK_SPIN, false, MODE, V, TMA>;
+      case P_EBO_MUTEX: return k_mutex<MK_EBO, false, MODE, V, TMA>;
+      case P_SLEEP_MUTEX: return k_mutex<MK_SLEEP, false, MODE, V, TMA>;
+      case P_FA_MUTEX: return k_mutex<MK_FA, false, MODE, V, TMA>;
+      case P_SPIN_MUTEX_UNIQ: return k_mutex<MK_SPIN, true, MODE, V, TMA>;
+      case P_EBO_MUTEX_UNIQ: return k_mutex<MK_EBO, true, MODE, V, TMA>;
+      case P_SLEEP_MUTEX_UNIQ: return k_mutex<MK_SLEEP, true, MODE, V, TMA>;
+      case P_FA_MUTEX_UNIQ: return k_mutex<MK_FA, true, MODE, V, TMA>;
+      default: return nullptr;
+    }
+  } else {
+    switch (prim) {
+      case P_SPIN_MUTEX: return k_mutex<MK_SPIN, false, MODE, V>;
+      case P_EBO_MUTEX: return k_mutex<MK_EBO, false, MODE, V>;
+      case P_SLEEP_MUTEX: return k_mutex<MK_SLEEP, false, MODE, V>;
+      case P_FA_MUTEX: return k_mutex<MK_FA, false, MODE, V>;
+      case P_SPIN_MUTEX_UNIQ: return k_mutex<MK_SPIN, true, MODE, V>;
+      case P_EBO_MUTEX_UNIQ: return k_mutex<MK_EBO, true, MODE, V>;
+      case P_SLEEP_MUTEX_UNIQ: return k_mutex<MK_SLEEP, true, MODE, V>;
+      case P_FA_MUTEX_UNIQ: return k_mutex<MK_FA, true, MODE, V>;
+      default: return nullptr;
+    }
   }
 }
 
-template <int V>
+template <int V, bool TMA>
 static KernelFn pick_v(int prim, int mode) {
   switch (mode) {
-    case M_REF: return pick<M_REF, V>(prim);
-    case M_INC: return pick<M_INC, V>(prim);
-    case M_SLICE: return pick<M_SLICE, V>(prim);
+    case M_REF: return pick<M_REF, V, TMA>(prim);
+    case M_INC: return pick<M_INC, V, TMA>(prim);
+    case M_SLICE: return TMA ? nullptr : pick<M_SLICE, V, false>(prim);
     default: return nullptr;
   }
 }
 
-// Deepest vector variant that the thread count (and, for barriers, the
-// co-residency the caller checks) allows.
-KernelFn syncprim_kernel(int prim, int mode, int threads, int num_ldst) {
+// Kernel choice for a run.  Mutex and semaphore kernels with numLdSt > 32 whose
+// chunk fits in shared memory take the TMA path (dynamic shared memory = one
+// chunk); otherwise the register path with the deepest vector variant the
+// thread count allows.  Barrier kernels always take the register path (all TBs
+// must be co-resident).
+KernelFn syncprim_plan(int prim, int mode, int threads, int num_ldst, size_t* smem_bytes) {
   const bool barrier = prim >= P_ATOMIC_TREE && prim <= P_LF_TREE_EXCH;
-  if (threads > 512) return pick_v<4>(prim, mode);
-  if (threads > 256 || barrier || num_ldst <= 32) return pick_v<8>(prim, mode);
-  return pick_v<26>(prim, mode);
+  const size_t chunk = (size_t)threads * (num_ldst + 1) * 4;
+  *smem_bytes = 0;
+  if (!barrier && mode != M_SLICE && threads <= 256 && num_ldst > 32 && chunk <= kTmaMaxBytes) {
+    *smem_bytes = chunk;
+    return pick_v<8, true>(prim, mode);
+  }
+  if (threads > 512) return pick_v<4, false>(prim, mode);
+  return pick_v<8, false>(prim, mode);
+}
+
+KernelFn syncprim_kernel(int prim, int mode, int threads, int num_ldst) {
+  size_t smem = 0;
+  return syncprim_plan(prim, mode, threads, num_ldst, &smem);
+}
+
+// Allow the kernel its dynamic shared memory (once per function).
+cudaError_t prepare_smem(KernelFn fn, size_t smem_bytes) {
+  if (smem_bytes <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTmaMaxBytes);
 }
 
 __global__ void k_fill_lines(unsigned* base, size_t n, size_t stride, unsigned value) {

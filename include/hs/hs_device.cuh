@@ -41,7 +41,7 @@ enum : unsigned {
   HS_SITE_SPIN_LOCK = 1, HS_SITE_EBO_LOCK = 2, HS_SITE_FA_LOCK = 3, HS_SITE_SLEEP_LOCK = 4,
   HS_SITE_SEM_WAIT = 5, HS_SITE_BAR_LOCAL = 6, HS_SITE_BAR_GLOBAL = 7, HS_SITE_BAR_SCAN = 8,
   HS_SITE_BAR_GO = 9, HS_SITE_BATCH = 10, HS_SITE_SERVE = 11, HS_SITE_RELAXED = 12,
-  HS_SITE_UTS = 13, HS_SITE_EXCH = 14,
+  HS_SITE_UTS = 13, HS_SITE_EXCH = 14, HS_SITE_TMA = 15,
 };
 
 struct HsEnv {
