@@ -20,7 +20,7 @@ CASES = [
     (256, 10, 6, 1, 1, 3),    # BASELINE thread count
     (64, 25, 5, 2, 1, 8),     # fewer TBs than SMs
     (16, 12, 12, 1, 1, 4),    # 3 TBs per logical SM, half-warp TBs
-    (256, 100, 3, 2, 1, 2),   # 100 KB chunks: bulk-copy (TMA) critical sections
+    (256, 100, 4, 2, 1, 2),   # 100 KB chunks: bulk-copy (TMA) critical sections
 ]
 
 
