@@ -172,6 +172,17 @@ extern "C" int hs_ref_run(const char* cubin, int T, int prim, int L, int numTBs,
     g_msg = "reference Uniq semaphore kernels livelock on this GPU (stale per-SM count reads); not run";
     return 3;
   }
+  if (rp->kind == 2) {
+    // The reference's global semaphore kernels (kernelSpinLockSemaphore /
+    // kernelEBOSemaphore) read maxSemCount from the live count word at kernel
+    // start (main.cu:542-543, 695-696).  A CTA that starts after another writer
+    // took the semaphore reads 0; as a writer it then waits for count == 0,
+    // which never recurs once every other writer has finished.  A bench run
+    // whose reference arm launched them did not finish (killed after 600 s).
+    // Never launched again.
+    g_msg = "reference global semaphore kernels can wait forever on GB300 (maxSemCount race at kernel start); not run";
+    return 3;
+  }
   if (rp->kind == 0) {
     if (!(numTBs <= NUM_SM || numTBs % NUM_SM == 0)) {
       g_msg = "barrier numTBs neither <= NUM_SM nor a multiple of it: the reference kernel would deadlock";

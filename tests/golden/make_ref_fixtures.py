@@ -24,9 +24,8 @@ CASES = [
     (6, 32, 25, (0, 2), 1, 10), (7, 256, 30, (0, 3), 1, 10), (4, 256, 12, (0, 1), 1, 10),
     (20, 32, 25, (1, 8), 1, 10), (21, 32, 25, (1, 8), 1, 10), (22, 32, 25, (1, 8), 1, 10),
     (23, 32, 25, (1, 8), 1, 10), (23, 256, 25, (1, 8), 1, 10),
-    (8, 32, 25, (2, 0), 1, 1), (9, 32, 25, (2, 0), 1, 1), (10, 32, 25, (1, 0), 2, 1),
-    (11, 32, 25, (0, 5), 1, 2), (12, 32, 25, (2, 0), 1, 1), (13, 32, 25, (2, 0), 1, 1),
-    (14, 32, 25, (1, 0), 2, 1), (15, 32, 25, (0, 5), 1, 2), (10, 256, 25, (2, 0), 1, 1),
+    # the reference's semaphore kernels (8-15, 24-31) are no longer run: see oracle/ref_runner.cpp;
+    # the committed fixture keeps the digests recorded for 8-15 before that
     # the reference's Uniq semaphore kernels (24-31) are not run: they livelocked on GB300
     (0, 32, 25, (1, 0), 2, 10), (1, 32, 45, (2, 0), 2, 10), (2, 32, 25, (1, 0), 2, 10),
     (3, 32, 45, (2, 0), 2, 10), (0, 256, 25, (2, 0), 2, 10), (1, 256, 45, (4, 0), 2, 10),

@@ -12,7 +12,7 @@ def _need_ref(oracle, T):
         pytest.skip("reference modules (oracle/_ref) not present")
 
 
-@pytest.mark.parametrize("prim", [0, 1, 2, 3, 4, 5, 6, 7, 8, 10, 12, 15, 20, 21, 22, 23])
+@pytest.mark.parametrize("prim", [0, 1, 2, 3, 4, 5, 6, 7, 20, 21, 22, 23])
 def test_reference_kernels_match_oracle_and_build(hs, oracle, prim):
     _need_ref(oracle, 32)
     nsm, _ = oracle.ref_device()
@@ -21,9 +21,6 @@ def test_reference_kernels_match_oracle_and_build(hs, oracle, prim):
         G, L, iters = 2 * nsm, 45, 2
     elif prim <= 7:
         G, L, iters = 2, 25, 1
-    elif prim <= 15:
-        G, L, iters = 2 * nsm, 25, 1
-        reps = 1
     else:
         G, L, iters = nsm + 8, 25, 1
     n = oracle.storage_words(prim, T, L, G, nsm)
@@ -62,3 +59,13 @@ def test_reference_runner_refuses_uniq_semaphores(oracle):
     init = np.zeros(oracle.storage_words(24, 32, 2, 4, 152), dtype=np.uint32)
     with pytest.raises(RuntimeError, match="livelock"):
         oracle.ref_run(24, 32, 2, 4, 1, 1, init)
+
+
+@pytest.mark.parametrize("prim", [8, 12])
+def test_reference_runner_refuses_global_semaphores(oracle, prim):
+    """The reference's global semaphore kernels can wait forever (maxSemCount is
+    read from the live count at kernel start); the runner refuses them."""
+    _need_ref(oracle, 32)
+    init = np.zeros(oracle.storage_words(prim, 32, 2, 4, 152), dtype=np.uint32)
+    with pytest.raises(RuntimeError, match="maxSemCount"):
+        oracle.ref_run(prim, 32, 2, 4, 1, 1, init)
