@@ -272,3 +272,127 @@ def run(cfg: RunConfig, storage, stream: Optional[int] = None, check: bool = Tru
     if check and s:
         raise _err(s)
     return res
+
+
+# ---------------------------------------------------------------------------
+# Relaxed-atomics microbenchmarks and UTS (include/hs/hs.h)
+# ---------------------------------------------------------------------------
+class _RelaxedResult(ctypes.Structure):
+    _fields_ = [("elapsed_ms", ctypes.c_float), ("ops", ctypes.c_ulonglong), ("dev_error_bits", ctypes.c_uint),
+                ("dev_error_site", ctypes.c_uint)]
+
+
+class _UtsResult(ctypes.Structure):
+    _fields_ = [("nodes_processed", ctypes.c_uint), ("leaves_found", ctypes.c_uint), ("leaf_sum", ctypes.c_uint),
+                ("elapsed_ms", ctypes.c_float), ("dev_error_bits", ctypes.c_uint)]
+
+
+def _np():
+    import numpy as np
+    return np
+
+
+def _relaxed_err(s):
+    L = lib()
+    L.hs_relaxed_last_error.restype = ctypes.c_char_p
+    return HsError(s, L.hs_relaxed_last_error().decode())
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def refcounter(num_sharers: int, num_tbs: int, tb_size: int, num_repeats: int):
+    """refCounter.cu: returns (counters0, counters1, del0, del1, result)."""
+    np = _np()
+    thr = num_tbs * tb_size
+    nc = thr // num_sharers
+    c0, c1 = np.zeros(nc, np.uint32), np.zeros(nc, np.uint32)
+    d0, d1 = np.zeros(thr, np.uint32), np.zeros(thr, np.uint32)
+    r = _RelaxedResult()
+    s = lib().hs_refcounter(num_sharers, num_tbs, tb_size, num_repeats, _p(c0), _p(c1), _p(d0), _p(d1), ctypes.byref(r))
+    if s:
+        raise _relaxed_err(s)
+    return c0, c1, d0, d1, r
+
+
+def splitcounter(num_tbs: int, tb_size: int):
+    """splitCounter.cu: returns (counters, outArr, result)."""
+    np = _np()
+    thr = num_tbs * tb_size
+    c, o = np.zeros(thr // 2, np.uint32), np.zeros(thr, np.uint32)
+    r = _RelaxedResult()
+    s = lib().hs_splitcounter(num_tbs, tb_size, _p(c), _p(o), ctypes.byref(r))
+    if s:
+        raise _relaxed_err(s)
+    return c, o, r
+
+
+def seqlocks(num_tbs: int, tb_size: int, group_size: int, use_tfs: bool = False, timeout_ns: int = 0):
+    """seqlocks.cu: returns (seqlock, data0, data1, outArr, result)."""
+    np = _np()
+    seq = np.zeros(max(num_tbs // group_size, 1), np.uint32)
+    d0, d1 = np.zeros(32, np.int32), np.zeros(32, np.int32)
+    o = np.full(num_tbs * tb_size, -1, np.int32)
+    r = _RelaxedResult()
+    lib().hs_seqlocks.argtypes = [ctypes.c_int] * 4 + [ctypes.c_void_p] * 4 + [ctypes.c_ulonglong, ctypes.c_void_p]
+    s = lib().hs_seqlocks(num_tbs, tb_size, group_size, int(use_tfs), _p(seq), _p(d0), _p(d1), _p(o), timeout_ns,
+                          ctypes.byref(r))
+    if s:
+        raise _relaxed_err(s)
+    return seq, d0, d1, o, r
+
+
+def flags(num_tbs: int, tb_size: int, num_accs: int, num_repeats: int, cutoff: float, num_iters: int, rand_arr):
+    """flags.cu: returns (outArr, dirty, result)."""
+    np = _np()
+    rand_arr = np.ascontiguousarray(rand_arr, dtype=np.float32)
+    o = np.zeros(num_tbs * tb_size, np.uint32)
+    dirty = ctypes.c_uint()
+    r = _RelaxedResult()
+    lib().hs_flags.argtypes = [ctypes.c_int] * 4 + [ctypes.c_float, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_ulonglong,
+                                                     ctypes.c_void_p]
+    s = lib().hs_flags(num_tbs, tb_size, num_accs, num_repeats, cutoff, num_iters, _p(rand_arr), rand_arr.size, _p(o),
+                       ctypes.byref(dirty), 0, ctypes.byref(r))
+    if s:
+        raise _relaxed_err(s)
+    return o, dirty.value, r
+
+
+UTS_NODE_FIELDS = [("value", "<u4"), ("depth", "<u4"), ("to_add", "<u4"), ("child_a", "<i4"), ("child_b", "<i4")]
+
+
+def uts_tree(num_nodes: int, fertility: int, seed: int = 200):
+    """uts.cu:290-339: (tree, golden leaves, golden leaf sum, restarts)."""
+    np = _np()
+    tree = np.zeros(num_nodes, dtype=np.dtype(UTS_NODE_FIELDS))
+    lv, ls, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint()
+    s = lib().hs_uts_tree_build(num_nodes, fertility, ctypes.c_uint(seed), _p(tree), ctypes.byref(lv),
+                                ctypes.byref(ls), ctypes.byref(rs))
+    if s:
+        raise HsError(s, "uts tree")
+    return tree, lv.value, ls.value, rs.value
+
+
+def uts_frontier(tree, cores_used: int):
+    np = _np()
+    fr = np.zeros(cores_used * 16 + 2, dtype=np.int32)
+    cnt, proc = ctypes.c_int(), ctypes.c_uint()
+    s = lib().hs_uts_frontier(_p(tree), tree.size, cores_used, _p(fr), ctypes.byref(cnt), ctypes.byref(proc))
+    if s:
+        raise HsError(s, "uts frontier")
+    return fr[:cnt.value].copy(), proc.value
+
+
+def uts_run(tree, frontier, host_processed: int, blocks: int, threads: int = 128, timeout_ns: int = 0):
+    np = _np()
+    frontier = np.ascontiguousarray(frontier, dtype=np.int32)
+    r = _UtsResult()
+    lib().hs_uts_run.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint,
+                                 ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong, ctypes.c_void_p]
+    s = lib().hs_uts_run(_p(tree), tree.size, _p(frontier), frontier.size, host_processed, blocks, threads,
+                         timeout_ns, ctypes.byref(r))
+    if s:
+        raise HsError(s, "uts run")
+    return r

@@ -34,11 +34,17 @@ CU_SOURCES = [
     "hs_api.cu",
     "hs_probe.cu",
     "hs_noalloc.cu",
+    "hs_relaxed.cu",
+    "hs_relaxed_api.cu",
+    "hs_uts.cu",
 ]
 # command-line programs: (output name, source)
 PROGRAMS = [
     ("allSyncPrims-1kernel", "allSyncPrims.cpp"),
+    ("hs-relaxed", "relaxed_cli.cpp"),
 ]
+# names the multi-call relaxed-atomics/UTS program answers to (the reference's binaries)
+RELAXED_NAMES = ["refCounter", "splitCounter", "seqlocks", "flags", "uts"]
 
 
 def cuda_home() -> str:
@@ -100,6 +106,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
         if force or _stale(exe, [s, lib] + headers):
             _run(["g++", "-std=c++17", "-O2", "-I" + INC, s, "-o", exe, "-L" + LIB, "-lhsgb300",
                   "-Wl,-rpath,$ORIGIN/../lib"])
+    for alias in RELAXED_NAMES:
+        dst = os.path.join(BIN, alias)
+        if not os.path.exists(dst) or os.path.getmtime(dst) < os.path.getmtime(os.path.join(BIN, "hs-relaxed")):
+            if os.path.lexists(dst):
+                os.remove(dst)
+            shutil.copy2(os.path.join(BIN, "hs-relaxed"), dst)
     if verbose:
         print("built", lib)
     return lib

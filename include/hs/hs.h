@@ -133,6 +133,53 @@ int hs_expected_storage(const hs_run_config* cfg, int nsm, const uint32_t* init,
 int hs_run_noalloc(const hs_run_config* cfg, void* storage, void* stream, hs_run_result* result);
 const char* hs_noalloc_last_error(void);
 
+/* ---- relaxed-atomics microbenchmarks (cuda/relaxedAtomics/uvm/*) --------------- */
+/* Host arrays in and out (the reference's managed arrays); the kernel alone is
+ * timed.  Sizes and array lengths are the reference's. */
+typedef struct hs_relaxed_result {
+  float elapsed_ms;
+  unsigned long long ops;
+  unsigned dev_error_bits, dev_error_site;
+} hs_relaxed_result;
+const char* hs_relaxed_last_error(void);
+/* refCounter.cu:5-155: counters0/1 [numTBs*tbSize/numSharersPerGroup], del0/1 [numTBs*tbSize] */
+int hs_refcounter(int numSharersPerGroup, int numTBs, int tbSize, int numRepeats, unsigned* counters0,
+                  unsigned* counters1, unsigned* del0, unsigned* del1, hs_relaxed_result* result);
+/* splitCounter.cu:5-98: counters [numTBs*tbSize/2], outArr [numTBs*tbSize] */
+int hs_splitcounter(int numTBs, int tbSize, unsigned* counters, unsigned* outArr, hs_relaxed_result* result);
+/* seqlocks.cu:5-111: seqlock [numTBs/groupSize], data0/1 [32], outArr [numTBs*tbSize] */
+int hs_seqlocks(int numTBs, int tbSize, int groupSize, int useTFs, unsigned* seqlock, int* data0, int* data1,
+                int* outArr, unsigned long long timeout_ns, hs_relaxed_result* result);
+/* flags.cu:19-176: randArr [randLen], outArr [numTBs*tbSize], *dirty_out = final dirty count */
+int hs_flags(int numTBs, int tbSize, int numAccsPerThr, int numRepeats, float cutoffVal, int numIters,
+             const float* randArr, int randLen, unsigned* outArr, unsigned* dirty_out, unsigned long long timeout_ns,
+             hs_relaxed_result* result);
+
+/* ---- UTS (cuda/uts/uvm/uts.cu) -------------------------------------------------- */
+/* Same layout as the reference's uts_node (uts.cu:40-46). */
+typedef struct hs_uts_node {
+  unsigned int value;
+  unsigned int depth;
+  unsigned int to_add;
+  int child_a;
+  int child_b;
+} hs_uts_node;
+typedef struct hs_uts_result {
+  unsigned nodes_processed, leaves_found, leaf_sum;
+  float elapsed_ms;
+  unsigned dev_error_bits;
+} hs_uts_result;
+const char* hs_uts_last_error(void);
+/* uts.cu:290-339: binary tree of num_nodes (odd) nodes from srand(seed); golden leaf count and sum. */
+int hs_uts_tree_build(int num_nodes, int fertility, unsigned seed, hs_uts_node* tree, unsigned* leaves,
+                      unsigned* leaf_sum, unsigned* restarts);
+/* uts.cu:341-383: initial frontier of cores_used*16 nodes and the internal nodes expanded on the host. */
+int hs_uts_frontier(const hs_uts_node* tree, int num_nodes, int cores_used, int* frontier, int* count,
+                    unsigned* host_processed);
+/* Replaces access_shared (uts.cu:91-242): process every remaining node on the GPU. */
+int hs_uts_run(const hs_uts_node* tree, int num_nodes, const int* frontier, int n_frontier, unsigned host_processed,
+               int blocks, int threads, unsigned long long timeout_ns, hs_uts_result* out);
+
 /* ---- roofline probes --------------------------------------------------------- */
 /* Aggregate L2 atomic rate: blocks x threads threads each issue `iters`
  * red.add to their own 128-byte-spaced word (same_address = 0: contention-free

@@ -135,3 +135,31 @@ def twin_run(prim: int, T: int, L: int, num_tbs: int, iters: int, repeats: int, 
     if rc:
         raise ValueError("twin rejected the configuration")
     return s, float(secs.value)
+
+
+# ---------------------------------------------------------------------------
+# UTS (uts.c): reference tree generator, golden and initial frontier.
+# ---------------------------------------------------------------------------
+UTS_NODE = np.dtype([("value", "<u4"), ("depth", "<u4"), ("to_add", "<u4"), ("child_a", "<i4"), ("child_b", "<i4")])
+
+
+def uts_tree(num_nodes: int, fertility: int, seed: int = 200):
+    L_ = lib()
+    tree = np.zeros(num_nodes, dtype=UTS_NODE)
+    lv, ls, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint()
+    rc = L_.hs_oracle_uts_tree(num_nodes, fertility, ctypes.c_uint(seed), tree.ctypes.data, ctypes.byref(lv),
+                               ctypes.byref(ls), ctypes.byref(rs))
+    if rc:
+        raise ValueError("bad UTS tree size")
+    return tree, lv.value, ls.value, rs.value
+
+
+def uts_frontier(tree, cores_used: int):
+    L_ = lib()
+    fr = np.zeros(cores_used * 16 + 2, dtype=np.int32)
+    cnt, proc = ctypes.c_int(), ctypes.c_uint()
+    rc = L_.hs_oracle_uts_frontier(tree.ctypes.data, tree.size, cores_used, fr.ctypes.data, ctypes.byref(cnt),
+                                   ctypes.byref(proc))
+    if rc:
+        raise ValueError("frontier cannot be filled")
+    return fr[:cnt.value].copy(), proc.value
