@@ -396,3 +396,102 @@ def uts_run(tree, frontier, host_processed: int, blocks: int, threads: int = 128
     if s:
         raise HsError(s, "uts run")
     return r
+
+
+# ---------------------------------------------------------------------------
+# Batched mixed instances (hs_batch_*)
+# ---------------------------------------------------------------------------
+class _BatchInst(ctypes.Structure):
+    _fields_ = [("prim", ctypes.c_int), ("num_ldst", ctypes.c_int), ("num_tbs", ctypes.c_int),
+                ("num_iters", ctypes.c_int)]
+
+
+class _BatchResult(ctypes.Structure):
+    _fields_ = [("elapsed_ms", ctypes.c_float), ("ops", ctypes.c_ulonglong), ("launches", ctypes.c_uint),
+                ("grid", ctypes.c_int), ("tbs_per_cta", ctypes.c_int), ("dev_error_bits", ctypes.c_uint),
+                ("failed_instance", ctypes.c_int)]
+
+
+def batch_generate(seed: int, n: int = 64, nsm: int = 0, iter_div: int = 1):
+    """The BASELINE mixed batch: list of (prim, num_ldst, num_tbs, num_iters)."""
+    nsm = nsm or device_info()["nsm"]
+    arr = (_BatchInst * n)()
+    s = lib().hs_batch_generate(ctypes.c_ulonglong(seed), n, nsm, iter_div, arr)
+    if s:
+        raise HsError(s, "batch generate")
+    return [(a.prim, a.num_ldst, a.num_tbs, a.num_iters) for a in arr]
+
+
+class Batch:
+    """Instances run in one persistent, graph-replayed launch (run) or one
+    standalone launch each (run_serial)."""
+
+    def __init__(self, instances, mode: str = "inc"):
+        L = lib()
+        L.hs_batch_last_error.restype = ctypes.c_char_p
+        L.hs_batch_storage_words.restype = ctypes.c_size_t
+        L.hs_batch_storage_words.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        for f in ("hs_batch_set_storage", "hs_batch_get_storage"):
+            getattr(L, f).argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        for f in ("hs_batch_run", "hs_batch_run_serial"):
+            getattr(L, f).argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.hs_batch_plan.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        L.hs_batch_autotune.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.hs_batch_destroy.argtypes = [ctypes.c_void_p]
+        self.instances = list(instances)
+        arr = (_BatchInst * len(self.instances))(*[_BatchInst(*x) for x in self.instances])
+        h = ctypes.c_void_p()
+        s = L.hs_batch_create(arr, len(self.instances), 256, _MODES[mode], ctypes.byref(h))
+        if s:
+            raise HsError(s, L.hs_batch_last_error().decode())
+        self.h = h
+        self.mode = mode
+
+    def _check(self, s):
+        if s:
+            raise HsError(s, lib().hs_batch_last_error().decode())
+
+    def words(self, i):
+        return int(lib().hs_batch_storage_words(self.h, i))
+
+    def set_storage(self, i, arr):
+        import numpy as np
+        a = np.ascontiguousarray(arr, dtype=np.uint32)
+        self._check(lib().hs_batch_set_storage(self.h, i, a.ctypes.data))
+
+    def get_storage(self, i):
+        import numpy as np
+        a = np.empty(self.words(i), dtype=np.uint32)
+        self._check(lib().hs_batch_get_storage(self.h, i, a.ctypes.data))
+        return a
+
+    def plan(self, v):
+        grid, cap = ctypes.c_int(), ctypes.c_int()
+        s = lib().hs_batch_plan(self.h, v, ctypes.byref(grid), ctypes.byref(cap))
+        return s, grid.value, cap.value
+
+    def autotune(self):
+        v, ms = ctypes.c_int(), ctypes.c_float()
+        self._check(lib().hs_batch_autotune(self.h, None, ctypes.byref(v), ctypes.byref(ms)))
+        return v.value, ms.value
+
+    def run(self):
+        r = _BatchResult()
+        self._check(lib().hs_batch_run(self.h, None, ctypes.byref(r)))
+        return r
+
+    def run_serial(self):
+        r = _BatchResult()
+        self._check(lib().hs_batch_run_serial(self.h, None, ctypes.byref(r)))
+        return r
+
+    def close(self):
+        if self.h:
+            lib().hs_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

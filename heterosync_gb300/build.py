@@ -37,6 +37,7 @@ CU_SOURCES = [
     "hs_relaxed.cu",
     "hs_relaxed_api.cu",
     "hs_uts.cu",
+    "hs_batch.cu",
 ]
 # command-line programs: (output name, source)
 PROGRAMS = [

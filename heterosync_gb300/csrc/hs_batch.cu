@@ -1,0 +1,523 @@
+// hs_batch.cu -- many SyncPrims instances in one persistent launch.
+//
+// An instance is one run of one primitive (numTBs logical TBs, numLdSt,
+// numCSIters) with its own storage and lock state.  The batch kernel gives
+// instance i a gang of c_i co-resident CTAs and executes its numTBs logical TBs
+// on them: logical TB b runs on gang CTA b mod c_i, and a CTA works through its
+// logical TBs one operation at a time (iteration-major).  Synchronisation is the
+// instance's own: each operation acquires and releases the instance's lock or
+// semaphore; barrier instances join a counter barrier among the gang's CTAs
+// after every data phase.  Nothing waits on a logical TB that is not running
+// (a CTA takes a ticket, slot or semaphore only for the operation it is doing),
+// so any gang sizes are deadlock-free; barrier gangs are co-resident because
+// the whole grid is.
+//
+// The final storage of every instance equals the standalone run's (the same
+// critical sections touch the same chunks the same number of times), which the
+// tests check against the closed form of the reference golden.
+//
+// The launch (lock-state reset plus the persistent kernel) is captured once in
+// a CUDA graph and replayed.  hs_batch_run_serial() is the comparison point:
+// one standalone launch per instance on the same stream.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+#include "hs_cs.cuh"
+#include "../../include/hs/hs.h"
+
+void hs_note_launches(unsigned n);
+int hs_layout_for(const hs_run_config* c, int nsm, hs::Layout* out);
+
+namespace hs {
+using KernelFn = void (*)(RunDesc);
+KernelFn syncprim_plan(int prim, int mode, int threads, int num_ldst, size_t* smem_bytes);
+cudaError_t prepare_smem(KernelFn fn, size_t smem_bytes);
+cudaError_t launch_ring_init(unsigned* ring, unsigned slots_per_group, unsigned groups, cudaStream_t st);
+cudaError_t launch_fill_lines(unsigned* base, size_t n, size_t stride, unsigned value, cudaStream_t st);
+
+struct BatchInst {
+  RunDesc d;
+  int first_cta;  // first CTA of the gang
+  int gang;       // CTAs in the gang
+};
+
+__device__ __forceinline__ bool is_mutex_prim(int p) { return (p >= 4 && p <= 7) || (p >= 20 && p <= 23); }
+__device__ __forceinline__ bool is_sem_prim(int p) { return (p >= 8 && p <= 15) || (p >= 24 && p <= 31); }
+
+// One critical section of a mutex logical TB b at iteration j.
+template <int MODE>
+__device__ __noinline__ bool batch_mutex_op(const RunDesc& d, int b, int j, int* s_slot, const HsEnv& env) {
+  const bool uniq = d.prim >= 20;
+  const int kind = d.prim % 4;  // 0 spin, 1 EBO, 2 ring, 3 ticket (main.cu:1224-1256 order)
+  const int g = uniq ? (b % d.nsm) : 0;
+  unsigned* w0 = group_line(d, g, 0);
+  unsigned* w1 = group_line(d, g, 1);
+  unsigned* w2 = group_line(d, g, 2);
+  unsigned* ring = d.ring + (size_t)g * (d.ring_max + 1) * kRingStride;
+  const unsigned wrap = uniq ? 100000000u : 1000000000u;
+  bool ok;
+  int slot = 0;
+  if (kind == 0) ok = spin_lock<GPU>(w0, env);
+  else if (kind == 1) ok = ebo_lock<GPU>(w0, d.bo_min, d.bo_max, env);
+  else if (kind == 3) ok = ticket_lock<GPU>(w0, w1, wrap, d.bo_unit, d.bo_max, env);
+  else {
+    slot = queue_lock<GPU>(w2, ring, kRingStride, d.ring_max, d.bo_unit, env, s_slot);
+    ok = slot >= 0;
+  }
+  if (!ok) return false;
+  if (MODE == M_SLICE) {
+    const int G = uniq ? d.nsm : 1, r = b / G, m = (d.num_tbs - g + G - 1) / G;
+    cs_slice(d.data, g + ((r + j) % m) * G, d.L);
+  } else {
+    cs_chunk<MODE, 4>(d, g);
+  }
+  if (kind <= 1) spin_unlock<GPU>(w0);
+  else if (kind == 3) ticket_unlock<GPU>(w1, wrap);
+  else queue_unlock<GPU>(ring, kRingStride, d.ring_max, (unsigned)slot);
+  return true;
+}
+
+// One wait/CS/post of a semaphore logical TB b.
+template <int MODE>
+__device__ __noinline__ bool batch_sem_op(const RunDesc& d, int b, const HsEnv& env) {
+  const bool uniq = d.prim >= 24;
+  const bool ebo = (d.prim >= 12 && d.prim <= 15) || d.prim >= 28;
+  const int Gd = d.num_tbs;
+  const int numSM = Gd < d.nsm ? Gd : d.nsm;
+  const int smID = b % numSM, k = ceil_div(Gd, numSM), p = b / numSM;
+  const bool writer = (p == smID % k);
+  unsigned* st = group_line(d, uniq ? smID : 0, 0);
+  if (!sem_wait<GPU>(st, writer, d.sem_max, ebo, !uniq, d.bo_min, d.bo_max, env)) return false;
+  if (writer) {
+    int cur = uniq ? b : 0;
+    for (int j = 0; j < k; ++j) {
+      cs_chunk<MODE, 4>(d, cur);
+      cur = uniq ? (cur + numSM) % Gd : cur + 1;
+    }
+  } else {
+    cs_read(d.data + (size_t)(uniq ? b : p) * chunk_words(d.T, d.L), d.T, d.L, d.sink + b);
+  }
+  sem_post<GPU>(st, writer, d.sem_max);
+  return true;
+}
+
+// Counter barrier among the gang's CTAs (instance's global barrier lines).
+__device__ __forceinline__ bool gang_barrier(const RunDesc& d, unsigned n, unsigned& gen, const HsEnv& env) {
+  int ok = 1;
+  if (is_master()) {
+    bool okb = true;
+    counter_barrier<GPU>(d.locks + (size_t)(d.l_glob + 0) * kLineWords, d.locks + (size_t)(d.l_glob + 1) * kLineWords,
+                         n, gen, d.bo_unit, env, HS_SITE_BATCH, [] { return true; }, &okb);
+    ok = okb;
+  }
+  gen += 1u;
+  return __syncthreads_or(!ok) == 0;
+}
+
+// Tree-barrier instance: every logical TB's chunk once per phase, a gang
+// barrier after each phase (LocalExch: a second phase on the chunk
+// numBlocksAtBarr TBs ahead, main.cu:153-211).
+template <int MODE>
+__device__ __noinline__ void batch_barrier(const RunDesc& d, int rank, int c, unsigned gen, const HsEnv& env) {
+  const int G = d.num_tbs, nb = G < d.nsm ? G : d.nsm, kmax = ceil_div(G, nb);
+  const bool exch = (d.prim == 1 || d.prim == 3) && kmax > 1;
+  for (int e = 0; e < d.iters; ++e) {
+    const long long base = exch ? (long long)e * (nb + 1) : (long long)e;
+    for (int b = rank; b < G; b += c) cs_chunk<MODE, 4>(d, (int)((b + base) % G));
+    if (!gang_barrier(d, (unsigned)c, gen, env)) return;
+    if (exch) {
+      for (int b = rank; b < G; b += c) cs_chunk<MODE, 4>(d, (int)((b + base + nb) % G));
+      if (!gang_barrier(d, (unsigned)c, gen, env)) return;
+    }
+  }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256, 4) k_batch(const BatchInst* insts, int n_inst) {
+  __shared__ int s_slot;
+  __shared__ int s_inst;
+  __shared__ unsigned s_gen;
+  const int cta = blockIdx.x;
+  if (is_master()) {  // gang lookup: binary search over first_cta
+    int lo = 0, hi = n_inst - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) / 2;
+      if (insts[mid].first_cta <= cta) lo = mid;
+      else hi = mid - 1;
+    }
+    s_inst = lo;
+    s_gen = ld_relaxed<GPU>(insts[lo].d.locks + (size_t)(insts[lo].d.l_glob + 1) * kLineWords);
+  }
+  __syncthreads();
+  const BatchInst& bi = insts[s_inst];
+  const RunDesc d = bi.d;
+  const int rank = cta - bi.first_cta, c = bi.gang;
+  if (rank < 0 || rank >= c) return;
+  const HsEnv env{d.status, d.timeout_ns};
+  if (is_mutex_prim(d.prim)) {
+    for (int j = 0; j < d.iters; ++j)
+      for (int b = rank; b < d.num_tbs; b += c)
+        if (!batch_mutex_op<MODE>(d, b, j, &s_slot, env)) return;
+  } else if (is_sem_prim(d.prim)) {
+    for (int j = 0; j < d.iters; ++j)
+      for (int b = rank; b < d.num_tbs; b += c)
+        if (!batch_sem_op<MODE>(d, b, env)) return;
+  } else {
+    batch_barrier<MODE>(d, rank, c, s_gen, env);
+  }
+}
+
+}  // namespace hs
+
+using namespace hs;
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+struct hs_batch {
+  int n = 0, nsm = 0, threads = 256, mode = HS_MODE_INC;
+  std::vector<hs_batch_instance> inst;
+  std::vector<hs_run_config> cfg;
+  std::vector<size_t> words;
+  std::vector<Layout> lay;
+  std::vector<BatchInst> host_desc;
+  unsigned* storage = nullptr;   // all instances' storage, 256-byte aligned slices
+  std::vector<size_t> st_off;    // word offsets
+  unsigned* state = nullptr;     // all lock state, rings, sinks, status
+  size_t state_words = 0;
+  BatchInst* d_desc = nullptr;
+  int grid = 0, v = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  unsigned graph_kernels = 0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+};
+
+namespace {
+thread_local std::string g_berr;
+size_t round64(size_t w) { return (w + 63) / 64 * 64; }
+bool is_barrier_p(int p) { return p >= 0 && p <= 3; }
+bool is_usem_p(int p) { return p >= 24 && p <= 31; }
+}  // namespace
+
+extern "C" const char* hs_batch_last_error(void) { return g_berr.c_str(); }
+
+// The BASELINE mixed batch: instances drawn from std::mt19937_64(seed) in the
+// order primitive, numTBs, numLdSt, numCSIters; u = (draw >> 11) * 2^-53.
+// primitive uniform over the 28 SyncPrims, numTBs = round(exp(U(ln 4, ln 512))),
+// numLdSt = 1 + floor(128 u), numCSIters = 10 + floor(4991 u) divided by
+// iter_div (>= 1).  Barrier and per-SM-semaphore instances with numTBs above
+// NUM_SM are rounded to a multiple of NUM_SM (the reference defines those only
+// for whole SM groups: README.txt:80, main.cu:1775-1786).
+extern "C" int hs_batch_generate(unsigned long long seed, int n, int nsm, int iter_div, hs_batch_instance* out) {
+  static const int prims[28] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15,
+                                20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30, 31};
+  if (n <= 0 || nsm <= 0 || !out) return HS_EINVAL;
+  if (iter_div < 1) iter_div = 1;
+  std::mt19937_64 rng(seed);
+  auto u = [&] { return (double)(rng() >> 11) * (1.0 / 9007199254740992.0); };
+  for (int i = 0; i < n; ++i) {
+    hs_batch_instance& x = out[i];
+    x.prim = prims[std::min(27, (int)(u() * 28.0))];
+    int G = (int)std::lround(std::exp(std::log(4.0) + u() * (std::log(512.0) - std::log(4.0))));
+    if ((is_barrier_p(x.prim) || is_usem_p(x.prim)) && G > nsm) G = std::max(1, (int)std::lround((double)G / nsm)) * nsm;
+    x.num_tbs = G;
+    x.num_ldst = 1 + std::min(127, (int)(u() * 128.0));
+    x.num_iters = std::max(1, (10 + std::min(4990, (int)(u() * 4991.0))) / iter_div);
+  }
+  return HS_OK;
+}
+
+extern "C" int hs_batch_create(const hs_batch_instance* inst, int n, int threads, int mode, hs_batch** out) {
+  if (!inst || n <= 0 || !out || threads != 256 || (mode != HS_MODE_INC && mode != HS_MODE_REF)) {
+    g_berr = "need instances, 256 threads per TB and HS_MODE_INC or HS_MODE_REF";
+    return HS_EINVAL;
+  }
+  hs_batch* B = new hs_batch();
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&B->nsm, cudaDevAttrMultiProcessorCount, dev);
+  B->n = n;
+  B->threads = threads;
+  B->mode = mode;
+  B->inst.assign(inst, inst + n);
+  size_t st_total = 0, state_total = 0;
+  std::vector<size_t> state_off;
+  for (int i = 0; i < n; ++i) {
+    hs_run_config c;
+    hs_run_config_default(&c);
+    c.prim = inst[i].prim;
+    c.num_ldst = inst[i].num_ldst;
+    c.num_tbs = inst[i].num_tbs;
+    c.num_iters = inst[i].num_iters;
+    c.threads = threads;
+    c.repeats = 1;
+    c.mode = mode;
+    size_t w = 0;
+    int s = hs_storage_words(&c, B->nsm, &w);
+    if (s) { g_berr = hs_last_error(); delete B; return s; }
+    Layout L;
+    hs_layout_for(&c, B->nsm, &L);
+    B->cfg.push_back(c);
+    B->words.push_back(w);
+    B->lay.push_back(L);
+    B->st_off.push_back(st_total);
+    st_total += round64(w);
+    state_off.push_back(state_total);
+    state_total += 64 + round64((size_t)L.lines * kLineWords) + round64(L.ring_words) + round64((size_t)c.num_tbs);
+  }
+  if (cudaMalloc(&B->storage, st_total * 4 + 256) != cudaSuccess ||
+      cudaMalloc(&B->state, state_total * 4 + 256) != cudaSuccess ||
+      cudaMalloc(&B->d_desc, sizeof(BatchInst) * n) != cudaSuccess) {
+    cudaGetLastError();
+    g_berr = "cudaMalloc";
+    hs_batch_destroy(B);
+    return HS_ENORES;
+  }
+  cudaMemset(B->storage, 0, st_total * 4);
+  B->state_words = state_total;
+  for (int i = 0; i < n; ++i) {
+    const Layout& L = B->lay[i];
+    const hs_run_config& c = B->cfg[i];
+    RunDesc d;
+    std::memset(&d, 0, sizeof(d));
+    unsigned* base = B->state + state_off[i];
+    d.status = base;
+    d.locks = base + 64;
+    d.ring = d.locks + round64((size_t)L.lines * kLineWords);
+    d.sink = d.ring + round64(L.ring_words);
+    d.data = B->storage + B->st_off[i];
+    d.prim = c.prim;
+    d.mode = c.mode;
+    d.T = c.threads;
+    d.L = c.num_ldst;
+    d.num_tbs = c.num_tbs;
+    d.iters = c.num_iters;
+    d.nsm = B->nsm;
+    d.sem_max = (unsigned)hs_prim_sem_count(c.prim) + 1u;
+    d.bo_min = 1;
+    d.bo_max = 1024;
+    d.bo_unit = 0;
+    d.ring_max = (unsigned)c.num_tbs;
+    d.timeout_ns = 10000000000ull;
+    d.skip_tb = -1;
+    d.cluster = 1;
+    d.l_glob = L.l_glob;
+    d.l_gflag = L.l_gflag;
+    d.l_grp = L.l_grp;
+    d.l_lflag = L.l_lflag;
+    d.lflag_lines = L.lflag_lines;
+    BatchInst bi;
+    bi.d = d;
+    bi.first_cta = 0;
+    bi.gang = 1;
+    B->host_desc.push_back(bi);
+  }
+  cudaEventCreate(&B->e0);
+  cudaEventCreate(&B->e1);
+  *out = B;
+  return HS_OK;
+}
+
+extern "C" int hs_batch_destroy(hs_batch* B) {
+  if (!B) return HS_EINVAL;
+  if (B->exec) cudaGraphExecDestroy(B->exec);
+  if (B->graph) cudaGraphDestroy(B->graph);
+  cudaFree(B->storage);
+  cudaFree(B->state);
+  cudaFree(B->d_desc);
+  if (B->e0) cudaEventDestroy(B->e0);
+  if (B->e1) cudaEventDestroy(B->e1);
+  delete B;
+  return HS_OK;
+}
+
+extern "C" int hs_batch_set_storage(hs_batch* B, int i, const uint32_t* host) {
+  if (!B || i < 0 || i >= B->n) return HS_EINVAL;
+  return cudaMemcpy(B->storage + B->st_off[i], host, B->words[i] * 4, cudaMemcpyHostToDevice) == cudaSuccess
+             ? HS_OK : HS_ECUDA;
+}
+extern "C" int hs_batch_get_storage(hs_batch* B, int i, uint32_t* host) {
+  if (!B || i < 0 || i >= B->n) return HS_EINVAL;
+  return cudaMemcpy(host, B->storage + B->st_off[i], B->words[i] * 4, cudaMemcpyDeviceToHost) == cudaSuccess
+             ? HS_OK : HS_ECUDA;
+}
+extern "C" size_t hs_batch_storage_words(hs_batch* B, int i) {
+  return (!B || i < 0 || i >= B->n) ? 0 : B->words[i];
+}
+
+// Lock-state reset of every instance (semaphore counts, ring slots).
+static int reset_state(hs_batch* B, cudaStream_t st, unsigned* launches) {
+  if (cudaMemsetAsync(B->state, 0, B->state_words * 4, st) != cudaSuccess) return HS_ECUDA;
+  for (int i = 0; i < B->n; ++i) {
+    const RunDesc& d = B->host_desc[i].d;
+    if (d.sem_max > 1u) {
+      if (launch_fill_lines(d.locks + (size_t)B->lay[i].l_grp * kLineWords, (size_t)B->lay[i].groups,
+                            (size_t)4 * kLineWords, d.sem_max, st) != cudaSuccess)
+        return HS_ECUDA;
+      ++*launches;
+    }
+    if (d.prim == 6 || d.prim == 22) {
+      if (launch_ring_init(d.ring, d.ring_max + 1u, d.prim == 22 ? (unsigned)B->nsm : 1u, st) != cudaSuccess)
+        return HS_ECUDA;
+      ++*launches;
+    }
+  }
+  return HS_OK;
+}
+
+static int read_statuses(hs_batch* B, hs_batch_result* r) {
+  for (int i = 0; i < B->n; ++i) {
+    unsigned h[2] = {0, 0};
+    cudaMemcpy(h, B->host_desc[i].d.status, sizeof(h), cudaMemcpyDeviceToHost);
+    if (h[0]) {
+      r->dev_error_bits = h[0];
+      r->failed_instance = i;
+      g_berr = "instance " + std::to_string(i) + " device wait timed out";
+      return HS_ETIMEDOUT;
+    }
+  }
+  return HS_OK;
+}
+
+static unsigned long long total_ops(const hs_batch* B) {
+  unsigned long long o = 0;
+  for (const auto& c : B->cfg) o += (unsigned long long)c.num_tbs * c.num_iters;
+  return o;
+}
+
+// Gangs of ceil(numTBs / v) CTAs.  Returns the grid size, or 0 if it cannot be co-resident.
+extern "C" int hs_batch_plan(hs_batch* B, int v, int* grid_out, int* capacity_out) {
+  if (!B || v <= 0) return HS_EINVAL;
+  int per_sm = 0;
+  auto fn = B->mode == HS_MODE_INC ? k_batch<M_INC> : k_batch<M_REF>;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, B->threads, 0) != cudaSuccess) return HS_ECUDA;
+  const int cap = per_sm * B->nsm;
+  int grid = 0;
+  for (int i = 0; i < B->n; ++i) {
+    B->host_desc[i].first_cta = grid;
+    B->host_desc[i].gang = (B->cfg[i].num_tbs + v - 1) / v;
+    grid += B->host_desc[i].gang;
+  }
+  if (capacity_out) *capacity_out = cap;
+  if (grid_out) *grid_out = grid;
+  if (grid > cap) {
+    g_berr = "gangs need " + std::to_string(grid) + " co-resident CTAs, capacity " + std::to_string(cap);
+    return HS_ENORES;
+  }
+  if (B->exec) { cudaGraphExecDestroy(B->exec); B->exec = nullptr; }
+  if (B->graph) { cudaGraphDestroy(B->graph); B->graph = nullptr; }
+  B->grid = grid;
+  B->v = v;
+  if (cudaMemcpy(B->d_desc, B->host_desc.data(), sizeof(BatchInst) * B->n, cudaMemcpyHostToDevice) != cudaSuccess)
+    return HS_ECUDA;
+  return HS_OK;
+}
+
+// Capture (once per plan) and replay: lock-state reset + the persistent kernel.
+extern "C" int hs_batch_run(hs_batch* B, void* stream, hs_batch_result* r) {
+  std::memset(r, 0, sizeof(*r));
+  r->failed_instance = -1;
+  if (!B || !B->grid) { g_berr = "call hs_batch_plan first"; return HS_EINVAL; }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned launches = 0;
+  if (!B->exec) {
+    cudaStream_t cap;
+    if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return HS_ECUDA;
+    if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return HS_ECUDA;
+    unsigned n_init = 0;
+    int s = reset_state(B, cap, &n_init);
+    const BatchInst* dd = B->d_desc;
+    int ni = B->n;
+    void* args[] = {&dd, &ni};
+    const void* fn = B->mode == HS_MODE_INC ? (const void*)k_batch<M_INC> : (const void*)k_batch<M_REF>;
+    cudaError_t e = cudaLaunchKernel(fn, dim3(B->grid), dim3(B->threads), args, 0, cap);
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    if (s || e != cudaSuccess || e2 != cudaSuccess) {
+      g_berr = std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2);
+      if (g) cudaGraphDestroy(g);
+      return HS_ECUDA;
+    }
+    B->graph = g;
+    B->graph_kernels = n_init + 1u;
+    if (cudaGraphInstantiate(&B->exec, g, 0) != cudaSuccess) { g_berr = "graph instantiate"; return HS_ECUDA; }
+  }
+  launches = B->graph_kernels;
+  cudaEventRecord(B->e0, st);
+  if (cudaGraphLaunch(B->exec, st) != cudaSuccess) return HS_ECUDA;
+  cudaEventRecord(B->e1, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) { g_berr = "batch kernel failed"; return HS_ECUDA; }
+  hs_note_launches(launches);
+  cudaEventElapsedTime(&r->elapsed_ms, B->e0, B->e1);
+  r->launches = launches;
+  r->ops = total_ops(B);
+  r->grid = B->grid;
+  r->tbs_per_cta = B->v;
+  return read_statuses(B, r);
+}
+
+// The comparison point: one standalone launch per instance, same stream.
+extern "C" int hs_batch_run_serial(hs_batch* B, void* stream, hs_batch_result* r) {
+  std::memset(r, 0, sizeof(*r));
+  r->failed_instance = -1;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned launches = 0;
+  if (reset_state(B, st, &launches)) return HS_ECUDA;
+  std::vector<KernelFn> fns(B->n);
+  std::vector<size_t> smem(B->n);
+  for (int i = 0; i < B->n; ++i) {
+    fns[i] = syncprim_plan(B->cfg[i].prim, B->cfg[i].mode, B->threads, B->cfg[i].num_ldst, &smem[i]);
+    if (!fns[i] || prepare_smem(fns[i], smem[i]) != cudaSuccess) { g_berr = "no kernel"; return HS_EINVAL; }
+  }
+  cudaEventRecord(B->e0, st);
+  for (int i = 0; i < B->n; ++i) {
+    RunDesc d = B->host_desc[i].d;
+    void* args[] = {&d};
+    if (cudaLaunchKernel((const void*)fns[i], dim3(B->cfg[i].num_tbs), dim3(B->threads), args, smem[i], st) !=
+        cudaSuccess)
+      return HS_ECUDA;
+    ++launches;
+  }
+  cudaEventRecord(B->e1, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) { g_berr = "serial launches failed"; return HS_ECUDA; }
+  hs_note_launches(launches);
+  cudaEventElapsedTime(&r->elapsed_ms, B->e0, B->e1);
+  r->launches = launches;
+  r->ops = total_ops(B);
+  return read_statuses(B, r);
+}
+
+// Autotuner: try TBs-per-CTA v in {1, 2, 4, ...} whose gangs fit, time one
+// replay each on a copy of the initial storage, keep the fastest plan.
+extern "C" int hs_batch_autotune(hs_batch* B, void* stream, int* best_v, float* best_ms) {
+  if (!B) return HS_EINVAL;
+  std::vector<std::vector<uint32_t>> saved(B->n);
+  for (int i = 0; i < B->n; ++i) {
+    saved[i].resize(B->words[i]);
+    hs_batch_get_storage(B, i, saved[i].data());
+  }
+  int best = 0;
+  float best_t = 1e30f;
+  int max_g = 1;
+  for (const auto& c : B->cfg) max_g = std::max(max_g, c.num_tbs);
+  for (int v = 1; v <= max_g * 2; v *= 2) {
+    int grid = 0, cap = 0;
+    if (hs_batch_plan(B, v, &grid, &cap) != HS_OK) continue;
+    hs_batch_result r;
+    if (hs_batch_run(B, stream, &r) != HS_OK) continue;
+    if (r.elapsed_ms < best_t) { best_t = r.elapsed_ms; best = v; }
+    for (int i = 0; i < B->n; ++i) hs_batch_set_storage(B, i, saved[i].data());
+  }
+  if (!best) { g_berr = "no plan fits"; return HS_ENORES; }
+  hs_batch_plan(B, best, nullptr, nullptr);
+  if (best_v) *best_v = best;
+  if (best_ms) *best_ms = best_t;
+  return HS_OK;
+}

@@ -1,0 +1,245 @@
+// hs_cs.cuh -- critical-section bodies shared by the SyncPrims kernels and the
+// batched persistent kernel (heterosync cuda/syncPrims/uvm/main.cu:60-100).
+#pragma once
+#include <cuda_runtime.h>
+#include "hs_internal.h"
+#include "../../include/hs/hs_device.cuh"
+
+namespace hs {
+
+// ---------------------------------------------------------------------------
+// Critical-section bodies.  A "chunk" is the data of one reference TB: T/16
+// half-warp regions of (L+1) lines x 16 words (main.cu:60-72, 1304-1308).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ size_t chunk_words(int T, int L) { return (size_t)T * (L + 1); }
+
+// REF: line n+1 <- line n for n = L-1..0 in every region of the chunk.
+// Passes of up to 32 lines go from the top down; each pass loads everything
+// into registers, one CTA barrier, then stores.  Stores of a pass never touch
+// lines a later pass loads, and a later pass only overwrites lines an earlier
+// pass already loaded, so one barrier per pass suffices.
+template <int MAXV>
+__device__ __forceinline__ void cs_ref_shift(unsigned* chunk, int T, int L) {
+  const int R = T >> 4;
+  const int rw4 = (L + 1) * 4;
+  uint4* c4 = reinterpret_cast<uint4*>(chunk);
+  const int lpp = 4 * MAXV;  // lines per pass: MAXV*T items / (R regions * 4 vectors)
+  for (int hi = L; hi > 0; hi -= lpp) {
+    const int lo = hi - lpp > 0 ? hi - lpp : 0;
+    const int per_region = (hi - lo) * 4;
+    const int nitems = R * per_region;
+    uint4 v[MAXV];
+    int idx[MAXV];
+#pragma unroll
+    for (int u = 0; u < MAXV; ++u) {
+      const int t = threadIdx.x + u * T;
+      idx[u] = -1;
+      if (t < nitems) {
+        const int h = t / per_region;
+        idx[u] = h * rw4 + lo * 4 + (t - h * per_region);
+        v[u] = c4[idx[u]];
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < MAXV; ++u)
+      if (idx[u] >= 0) c4[idx[u] + 4] = v[u];
+  }
+}
+
+// INC: every word of lines 1..L of every region gets +1.
+template <int MAXV>
+__device__ __forceinline__ void cs_inc(unsigned* chunk, int T, int L) {
+  const int R = T >> 4;
+  const int rw4 = (L + 1) * 4;
+  const int per_region = L * 4;
+  const int nitems = R * per_region;
+  uint4* c4 = reinterpret_cast<uint4*>(chunk);
+  for (int base = 0; base < nitems; base += MAXV * T) {
+    uint4 v[MAXV];
+    int idx[MAXV];
+#pragma unroll
+    for (int u = 0; u < MAXV; ++u) {
+      const int t = base + threadIdx.x + u * T;
+      idx[u] = -1;
+      if (t < nitems) {
+        const int h = t / per_region;
+        idx[u] = h * rw4 + 4 + (t - h * per_region);
+        v[u] = c4[idx[u]];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < MAXV; ++u)
+      if (idx[u] >= 0) {
+        v[u].x += 1u; v[u].y += 1u; v[u].z += 1u; v[u].w += 1u;
+        c4[idx[u]] = v[u];
+      }
+  }
+}
+
+// SLICE: words [s*L, s*L+L) get +1, one thread per word.
+__device__ __forceinline__ void cs_slice(unsigned* data, int s, int L) {
+  unsigned* p = data + (size_t)s * L;
+  for (int w = threadIdx.x; w < L; w += blockDim.x) p[w] += 1u;
+}
+
+// Semaphore reader: load lines 0..L-1 of the chunk (main.cu:89-100); the loaded
+// values are folded into one word per TB so the loads are not dead.
+__device__ __forceinline__ void cs_read(const unsigned* chunk, int T, int L, unsigned* sink_slot) {
+  const int R = T >> 4;
+  const int rw4 = (L + 1) * 4;
+  const int per_region = L * 4;
+  const int nitems = R * per_region;
+  const uint4* c4 = reinterpret_cast<const uint4*>(chunk);
+  unsigned acc = 0;
+  for (int t = threadIdx.x; t < nitems; t += T) {
+    const int h = t / per_region;
+    const uint4 v = c4[h * rw4 + (t - h * per_region)];
+    acc += v.x ^ v.y ^ v.z ^ v.w;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
+  if ((threadIdx.x & 31) == 0 && acc == 0x9E3779B9u) *sink_slot = acc;  // practically never taken
+}
+
+// ---------------------------------------------------------------------------
+// TMA path for large chunks (numLdSt > 32, chunk <= kTmaMaxBytes): one
+// cp.async.bulk copies the whole chunk into shared memory (completion counted
+// on an mbarrier), then one bulk store per half-warp region writes lines
+// 0..L-1 back one line up (INC: lines 1..L after +1 in shared memory).  The
+// copy engine keeps the whole chunk in flight, which roughly doubles one SM's
+// throughput on the critical section over vector loads.
+// Ordering: the acquire (generic proxy) is followed by fence.proxy.async before
+// the bulk load; the bulk stores are completed (wait_group 0) and followed by
+// fence.proxy.async before the release.
+// ---------------------------------------------------------------------------
+constexpr unsigned kTmaMaxBytes = 200u * 1024u;
+
+struct TmaCtx {
+  unsigned char* buf;  // dynamic shared memory, chunk bytes
+  unsigned mbar;       // shared address of the mbarrier
+  unsigned phase;
+};
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void tma_init(TmaCtx& t, unsigned long long* mbar_storage, unsigned char* dyn) {
+  t.buf = dyn;
+  t.mbar = smem_addr(mbar_storage);
+  t.phase = 0;
+  if (is_master()) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(t.mbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ bool mbar_done(unsigned mbar, unsigned phase) {
+  unsigned done;
+  asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+               : "=r"(done) : "r"(mbar), "r"(phase) : "memory");
+  return done != 0;
+}
+
+// Load a chunk into shared memory; returns the CTA-wide success.
+__device__ __forceinline__ bool tma_load_chunk(const unsigned* chunk, unsigned bytes, TmaCtx& t, const HsEnv& env) {
+  if (is_master()) {
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(t.mbar), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(smem_addr(t.buf)), "l"(chunk), "r"(bytes), "r"(t.mbar) : "memory");
+  }
+  const bool ok = wait_until([&] { return mbar_done(t.mbar, t.phase); }, [] {}, env, HS_SITE_TMA);
+  t.phase ^= 1u;
+  return __syncthreads_and(ok) != 0;
+}
+
+// Store lines [first, first+L) of every region of the staged chunk to lines
+// [1, L] of the chunk in global memory, and complete the writes.
+__device__ __forceinline__ void tma_store_shifted(unsigned* chunk, int T, int L, unsigned first, TmaCtx& t) {
+  if (is_master()) {
+    const int R = T >> 4;
+    const unsigned rb = (unsigned)(16 * (L + 1) * 4);
+    const unsigned sbase = smem_addr(t.buf);
+    for (int h = 0; h < R; ++h) {
+      unsigned char* dst = reinterpret_cast<unsigned char*>(chunk) + (size_t)h * rb + 64u;
+      asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                   :: "l"(dst), "r"(sbase + h * rb + first * 64u), "r"((unsigned)(64 * L)) : "memory");
+    }
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+  }
+}
+
+template <int MODE>
+__device__ __forceinline__ bool cs_chunk_tma(const RunDesc& d, int chunk, TmaCtx& t, const HsEnv& env) {
+  unsigned* c = d.data + (size_t)chunk * chunk_words(d.T, d.L);
+  const unsigned bytes = (unsigned)(d.T * (d.L + 1) * 4);
+  if (!tma_load_chunk(c, bytes, t, env)) return false;
+  if constexpr (MODE == M_REF) {
+    tma_store_shifted(c, d.T, d.L, 0u, t);
+  } else {
+    const int R = d.T >> 4, per_region = d.L * 4, rw4 = (d.L + 1) * 4;
+    uint4* s4 = reinterpret_cast<uint4*>(t.buf);
+    for (int i = threadIdx.x; i < R * per_region; i += d.T) {
+      const int h = i / per_region;
+      uint4& v = s4[h * rw4 + 4 + (i - h * per_region)];
+      v.x += 1u; v.y += 1u; v.z += 1u; v.w += 1u;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic smem writes -> bulk store reads
+    __syncthreads();
+    // lines 1..L of smem go to lines 1..L of global: same offsets, so "shift" from line 1 to line 1
+    if (is_master()) {
+      const unsigned rb = (unsigned)(16 * (d.L + 1) * 4);
+      const unsigned sbase = smem_addr(t.buf);
+      for (int h = 0; h < R; ++h) {
+        unsigned char* dst = reinterpret_cast<unsigned char*>(c) + (size_t)h * rb + 64u;
+        asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                     :: "l"(dst), "r"(sbase + h * rb + 64u), "r"((unsigned)(64 * d.L)) : "memory");
+      }
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+      asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+      asm volatile("fence.proxy.async.global;" ::: "memory");
+    }
+  }
+  return true;
+}
+
+// Semaphore reader on the TMA path: stage the chunk, fold lines 0..L-1.
+__device__ __forceinline__ bool cs_read_tma(const RunDesc& d, int chunk, TmaCtx& t, const HsEnv& env,
+                                            unsigned* sink_slot) {
+  const unsigned* c = d.data + (size_t)chunk * chunk_words(d.T, d.L);
+  if (!tma_load_chunk(c, (unsigned)(d.T * (d.L + 1) * 4), t, env)) return false;
+  const int R = d.T >> 4, per_region = d.L * 4, rw4 = (d.L + 1) * 4;
+  const uint4* s4 = reinterpret_cast<const uint4*>(t.buf);
+  unsigned acc = 0;
+  for (int i = threadIdx.x; i < R * per_region; i += d.T) {
+    const int h = i / per_region;
+    const uint4 v = s4[h * rw4 + (i - h * per_region)];
+    acc += v.x ^ v.y ^ v.z ^ v.w;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
+  if ((threadIdx.x & 31) == 0 && acc == 0x9E3779B9u) *sink_slot = acc;
+  __syncthreads();  // the buffer is reused by the next load
+  return true;
+}
+
+// Vector depth V = 16-byte vectors each thread keeps in flight per pass.  The
+// launch bound follows from it: V 4 -> 1024 threads, 8 -> 512, 26 -> 256 (a
+// 256-thread TB then moves numLdSt <= 104 lines of its chunk in one pass).
+template <int V> struct Bounds { static constexpr int kThreads = V <= 4 ? 1024 : (V <= 8 ? 512 : 256); };
+
+template <int MODE, int V>
+__device__ __forceinline__ void cs_chunk(const RunDesc& d, int chunk) {
+  unsigned* c = d.data + (size_t)chunk * chunk_words(d.T, d.L);
+  if constexpr (MODE == M_REF) cs_ref_shift<V>(c, d.T, d.L);
+  else cs_inc<V>(c, d.T, d.L);
+}
+
+__device__ __forceinline__ unsigned* group_line(const RunDesc& d, int g, int k) {
+  return d.locks + (size_t)(d.l_grp + 4 * g + k) * kLineWords;
+}
+
+}  // namespace hs

@@ -133,6 +133,38 @@ int hs_expected_storage(const hs_run_config* cfg, int nsm, const uint32_t* init,
 int hs_run_noalloc(const hs_run_config* cfg, void* storage, void* stream, hs_run_result* result);
 const char* hs_noalloc_last_error(void);
 
+/* ---- batched mixed instances: one persistent, graph-replayed launch --------------- */
+/* No counterpart in the reference (its runs are one primitive per process).
+ * Instance i runs numTBs logical TBs on a gang of ceil(numTBs / v) co-resident
+ * CTAs; every instance has its own storage and lock state; 256 threads per TB. */
+typedef struct hs_batch_instance { int prim, num_ldst, num_tbs, num_iters; } hs_batch_instance;
+typedef struct hs_batch_result {
+  float elapsed_ms;             /* device time of the batch (or of all serial launches) */
+  unsigned long long ops;       /* sum of numTBs * numCSIters */
+  unsigned launches;            /* kernels launched */
+  int grid;                     /* CTAs of the persistent launch (0 for the serial form) */
+  int tbs_per_cta;              /* v */
+  unsigned dev_error_bits;
+  int failed_instance;          /* -1 if none */
+} hs_batch_result;
+typedef struct hs_batch hs_batch;
+const char* hs_batch_last_error(void);
+/* The mixed batch of BASELINE config 4, drawn from std::mt19937_64(seed). */
+int hs_batch_generate(unsigned long long seed, int n, int nsm, int iter_div, hs_batch_instance* out);
+int hs_batch_create(const hs_batch_instance* inst, int n, int threads, int mode, hs_batch** out);
+int hs_batch_destroy(hs_batch* b);
+size_t hs_batch_storage_words(hs_batch* b, int i);
+int hs_batch_set_storage(hs_batch* b, int i, const uint32_t* host);
+int hs_batch_get_storage(hs_batch* b, int i, uint32_t* host);
+/* Gang plan with v logical TBs per CTA; HS_ENORES if the gangs cannot be co-resident. */
+int hs_batch_plan(hs_batch* b, int v, int* grid, int* capacity);
+/* Try v = 1, 2, 4, ... and keep the fastest plan that fits (storage is restored after each try). */
+int hs_batch_autotune(hs_batch* b, void* stream, int* best_v, float* best_ms);
+/* Lock-state reset + persistent kernel, captured once per plan into a CUDA graph and replayed. */
+int hs_batch_run(hs_batch* b, void* stream, hs_batch_result* result);
+/* Comparison point: one standalone launch per instance on the same stream. */
+int hs_batch_run_serial(hs_batch* b, void* stream, hs_batch_result* result);
+
 /* ---- relaxed-atomics microbenchmarks (cuda/relaxedAtomics/uvm/*) --------------- */
 /* Host arrays in and out (the reference's managed arrays); the kernel alone is
  * timed.  Sizes and array lengths are the reference's. */
