@@ -50,8 +50,20 @@ __device__ __forceinline__ bool is_mutex_prim(int p) { return (p >= 4 && p <= 7)
 __device__ __forceinline__ bool is_sem_prim(int p) { return (p >= 8 && p <= 15) || (p >= 24 && p <= 31); }
 
 // One critical section of a mutex logical TB b at iteration j.
+// Batch critical section: tiled bulk copies through the CTA's staging buffer for
+// numLdSt > 16, vector loads otherwise.
+constexpr unsigned kBatchBuf = 40u * 1024u;
+
 template <int MODE>
-__device__ __noinline__ bool batch_mutex_op(const RunDesc& d, int b, int j, int* s_slot, const HsEnv& env) {
+__device__ __forceinline__ bool batch_cs(const RunDesc& d, int chunk, TmaCtx& t, const HsEnv& env) {
+  if (d.L > 16) return cs_chunk_tma_tiled<MODE>(d, chunk, t, kBatchBuf, env);
+  cs_chunk<MODE, 4>(d, chunk);
+  return true;
+}
+
+template <int MODE>
+__device__ __noinline__ bool batch_mutex_op(const RunDesc& d, int b, int j, int* s_slot, TmaCtx& t,
+                                            const HsEnv& env) {
   const bool uniq = d.prim >= 20;
   const int kind = d.prim % 4;  // 0 spin, 1 EBO, 2 ring, 3 ticket (main.cu:1224-1256 order)
   const int g = uniq ? (b % d.nsm) : 0;
@@ -70,21 +82,22 @@ __device__ __noinline__ bool batch_mutex_op(const RunDesc& d, int b, int j, int*
     ok = slot >= 0;
   }
   if (!ok) return false;
+  bool cs_ok = true;
   if (MODE == M_SLICE) {
     const int G = uniq ? d.nsm : 1, r = b / G, m = (d.num_tbs - g + G - 1) / G;
     cs_slice(d.data, g + ((r + j) % m) * G, d.L);
   } else {
-    cs_chunk<MODE, 4>(d, g);
+    cs_ok = batch_cs<MODE>(d, g, t, env);
   }
   if (kind <= 1) spin_unlock<GPU>(w0);
   else if (kind == 3) ticket_unlock<GPU>(w1, wrap);
   else queue_unlock<GPU>(ring, kRingStride, d.ring_max, (unsigned)slot);
-  return true;
+  return cs_ok;
 }
 
 // One wait/CS/post of a semaphore logical TB b.
 template <int MODE>
-__device__ __noinline__ bool batch_sem_op(const RunDesc& d, int b, const HsEnv& env) {
+__device__ __noinline__ bool batch_sem_op(const RunDesc& d, int b, TmaCtx& t, const HsEnv& env) {
   const bool uniq = d.prim >= 24;
   const bool ebo = (d.prim >= 12 && d.prim <= 15) || d.prim >= 28;
   const int Gd = d.num_tbs;
@@ -93,17 +106,18 @@ __device__ __noinline__ bool batch_sem_op(const RunDesc& d, int b, const HsEnv& 
   const bool writer = (p == smID % k);
   unsigned* st = group_line(d, uniq ? smID : 0, 0);
   if (!sem_wait<GPU>(st, writer, d.sem_max, ebo, !uniq, d.bo_min, d.bo_max, env)) return false;
+  bool ok = true;
   if (writer) {
     int cur = uniq ? b : 0;
-    for (int j = 0; j < k; ++j) {
-      cs_chunk<MODE, 4>(d, cur);
+    for (int j = 0; j < k && ok; ++j) {
+      ok = batch_cs<MODE>(d, cur, t, env);
       cur = uniq ? (cur + numSM) % Gd : cur + 1;
     }
   } else {
     cs_read(d.data + (size_t)(uniq ? b : p) * chunk_words(d.T, d.L), d.T, d.L, d.sink + b);
   }
   sem_post<GPU>(st, writer, d.sem_max);
-  return true;
+  return ok;
 }
 
 // Counter barrier among the gang's CTAs (instance's global barrier lines).
@@ -123,15 +137,18 @@ __device__ __forceinline__ bool gang_barrier(const RunDesc& d, unsigned n, unsig
 // barrier after each phase (LocalExch: a second phase on the chunk
 // numBlocksAtBarr TBs ahead, main.cu:153-211).
 template <int MODE>
-__device__ __noinline__ void batch_barrier(const RunDesc& d, int rank, int c, unsigned gen, const HsEnv& env) {
+__device__ __noinline__ void batch_barrier(const RunDesc& d, int rank, int c, unsigned gen, TmaCtx& t,
+                                           const HsEnv& env) {
   const int G = d.num_tbs, nb = G < d.nsm ? G : d.nsm, kmax = ceil_div(G, nb);
   const bool exch = (d.prim == 1 || d.prim == 3) && kmax > 1;
   for (int e = 0; e < d.iters; ++e) {
     const long long base = exch ? (long long)e * (nb + 1) : (long long)e;
-    for (int b = rank; b < G; b += c) cs_chunk<MODE, 4>(d, (int)((b + base) % G));
+    for (int b = rank; b < G; b += c)
+      if (!batch_cs<MODE>(d, (int)((b + base) % G), t, env)) return;
     if (!gang_barrier(d, (unsigned)c, gen, env)) return;
     if (exch) {
-      for (int b = rank; b < G; b += c) cs_chunk<MODE, 4>(d, (int)((b + base + nb) % G));
+      for (int b = rank; b < G; b += c)
+        if (!batch_cs<MODE>(d, (int)((b + base + nb) % G), t, env)) return;
       if (!gang_barrier(d, (unsigned)c, gen, env)) return;
     }
   }
@@ -142,6 +159,10 @@ __global__ void __launch_bounds__(256, 4) k_batch(const BatchInst* insts, int n_
   __shared__ int s_slot;
   __shared__ int s_inst;
   __shared__ unsigned s_gen;
+  __shared__ unsigned long long s_mbar;
+  extern __shared__ __align__(128) unsigned char dyn_smem[];
+  TmaCtx tma;
+  tma_init(tma, &s_mbar, dyn_smem);
   const int cta = blockIdx.x;
   if (is_master()) {  // gang lookup: binary search over first_cta
     int lo = 0, hi = n_inst - 1;
@@ -162,13 +183,13 @@ __global__ void __launch_bounds__(256, 4) k_batch(const BatchInst* insts, int n_
   if (is_mutex_prim(d.prim)) {
     for (int j = 0; j < d.iters; ++j)
       for (int b = rank; b < d.num_tbs; b += c)
-        if (!batch_mutex_op<MODE>(d, b, j, &s_slot, env)) return;
+        if (!batch_mutex_op<MODE>(d, b, j, &s_slot, tma, env)) return;
   } else if (is_sem_prim(d.prim)) {
     for (int j = 0; j < d.iters; ++j)
       for (int b = rank; b < d.num_tbs; b += c)
-        if (!batch_sem_op<MODE>(d, b, env)) return;
+        if (!batch_sem_op<MODE>(d, b, tma, env)) return;
   } else {
-    batch_barrier<MODE>(d, rank, c, s_gen, env);
+    batch_barrier<MODE>(d, rank, c, s_gen, tma, env);
   }
 }
 
@@ -396,7 +417,8 @@ extern "C" int hs_batch_plan(hs_batch* B, int v, int* grid_out, int* capacity_ou
   if (!B || v <= 0) return HS_EINVAL;
   int per_sm = 0;
   auto fn = B->mode == HS_MODE_INC ? k_batch<M_INC> : k_batch<M_REF>;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, B->threads, 0) != cudaSuccess) return HS_ECUDA;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, B->threads, kBatchBuf) != cudaSuccess)
+    return HS_ECUDA;
   const int cap = per_sm * B->nsm;
   int grid = 0;
   for (int i = 0; i < B->n; ++i) {
@@ -436,7 +458,7 @@ extern "C" int hs_batch_run(hs_batch* B, void* stream, hs_batch_result* r) {
     int ni = B->n;
     void* args[] = {&dd, &ni};
     const void* fn = B->mode == HS_MODE_INC ? (const void*)k_batch<M_INC> : (const void*)k_batch<M_REF>;
-    cudaError_t e = cudaLaunchKernel(fn, dim3(B->grid), dim3(B->threads), args, 0, cap);
+    cudaError_t e = cudaLaunchKernel(fn, dim3(B->grid), dim3(B->threads), args, kBatchBuf, cap);
     cudaGraph_t g = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(cap, &g);
     cudaStreamDestroy(cap);

@@ -206,6 +206,56 @@ __device__ __forceinline__ bool cs_chunk_tma(const RunDesc& d, int chunk, TmaCtx
   return true;
 }
 
+// Tiled TMA critical section: whole half-warp regions are independent, so a
+// chunk can be staged through a buffer smaller than the chunk, a tile of
+// regions at a time (one bulk load per tile, one bulk store per region).  Used
+// where shared memory must stay small (the batched kernel keeps four CTAs per
+// SM).  The buffer is reused only after the previous tile's stores have read
+// it (wait_group.read).
+template <int MODE>
+__device__ __forceinline__ bool cs_chunk_tma_tiled(const RunDesc& d, int chunk, TmaCtx& t, unsigned buf_bytes,
+                                                   const HsEnv& env) {
+  unsigned* c = d.data + (size_t)chunk * chunk_words(d.T, d.L);
+  const int R = d.T >> 4;
+  const unsigned rb = (unsigned)(64 * (d.L + 1));
+  int per = (int)(buf_bytes / rb);
+  if (per < 1) per = 1;
+  const unsigned sbase = smem_addr(t.buf);
+  for (int r0 = 0; r0 < R; r0 += per) {
+    const int n = (R - r0 < per) ? (R - r0) : per;
+    unsigned char* src = reinterpret_cast<unsigned char*>(c) + (size_t)r0 * rb;
+    if (!tma_load_chunk(reinterpret_cast<const unsigned*>(src), (unsigned)n * rb, t, env)) return false;
+    unsigned first = 0u;
+    if constexpr (MODE == M_INC) {
+      const int per_region = d.L * 4, rw4 = (d.L + 1) * 4;
+      uint4* s4 = reinterpret_cast<uint4*>(t.buf);
+      for (int i = threadIdx.x; i < n * per_region; i += d.T) {
+        const int h = i / per_region;
+        uint4& v = s4[h * rw4 + 4 + (i - h * per_region)];
+        v.x += 1u; v.y += 1u; v.z += 1u; v.w += 1u;
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+      first = 1u;
+    }
+    if (is_master()) {
+      for (int h = 0; h < n; ++h) {
+        asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                     :: "l"(src + (size_t)h * rb + 64u), "r"(sbase + h * rb + first * 64u), "r"((unsigned)(64 * d.L))
+                     : "memory");
+      }
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+      asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // buffer free for the next tile
+    }
+    __syncthreads();
+  }
+  if (is_master()) {
+    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");  // writes complete before the release
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+  }
+  return true;
+}
+
 // Semaphore reader on the TMA path: stage the chunk, fold lines 0..L-1.
 __device__ __forceinline__ bool cs_read_tma(const RunDesc& d, int chunk, TmaCtx& t, const HsEnv& env,
                                             unsigned* sink_slot) {
