@@ -470,6 +470,11 @@ class Batch:
         s = lib().hs_batch_plan(self.h, v, ctypes.byref(grid), ctypes.byref(cap))
         return s, grid.value, cap.value
 
+    def set_stage(self, nbytes: int):
+        """Staging bytes per CTA (0 = whole chunks); invalidates the plan."""
+        lib().hs_batch_set_stage.argtypes = [ctypes.c_void_p, ctypes.c_uint]
+        self._check(lib().hs_batch_set_stage(self.h, nbytes))
+
     def autotune(self):
         v, ms = ctypes.c_int(), ctypes.c_float()
         self._check(lib().hs_batch_autotune(self.h, None, ctypes.byref(v), ctypes.byref(ms)))

@@ -50,13 +50,17 @@ __device__ __forceinline__ bool is_mutex_prim(int p) { return (p >= 4 && p <= 7)
 __device__ __forceinline__ bool is_sem_prim(int p) { return (p >= 8 && p <= 15) || (p >= 24 && p <= 31); }
 
 // One critical section of a mutex logical TB b at iteration j.
-// Batch critical section: tiled bulk copies through the CTA's staging buffer for
-// numLdSt > 16, vector loads otherwise.
-constexpr unsigned kBatchBuf = 40u * 1024u;
+// Batch critical section: bulk copies through the CTA's staging buffer (the
+// whole chunk when it fits, else a tile of regions at a time) for numLdSt > 16,
+// vector loads otherwise.  The staging size is a launch parameter the
+// autotuner chooses (a small buffer keeps four CTAs per SM; a whole-chunk
+// buffer moves each chunk with one bulk load).
+constexpr unsigned kBatchBufSmall = 40u * 1024u;
+__constant__ unsigned c_stage_bytes;
 
 template <int MODE>
 __device__ __forceinline__ bool batch_cs(const RunDesc& d, int chunk, TmaCtx& t, const HsEnv& env) {
-  if (d.L > 16) return cs_chunk_tma_tiled<MODE>(d, chunk, t, kBatchBuf, env);
+  if (d.L > 16) return cs_chunk_tma_tiled<MODE>(d, chunk, t, c_stage_bytes, env);
   cs_chunk<MODE, 4>(d, chunk);
   return true;
 }
@@ -216,6 +220,7 @@ struct hs_batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   unsigned graph_kernels = 0;
+  unsigned stage = kBatchBufSmall;  // staging bytes per CTA
   cudaEvent_t e0 = nullptr, e1 = nullptr;
 };
 
@@ -417,7 +422,10 @@ extern "C" int hs_batch_plan(hs_batch* B, int v, int* grid_out, int* capacity_ou
   if (!B || v <= 0) return HS_EINVAL;
   int per_sm = 0;
   auto fn = B->mode == HS_MODE_INC ? k_batch<M_INC> : k_batch<M_REF>;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, B->threads, kBatchBuf) != cudaSuccess)
+  if (B->stage > 48u * 1024u &&
+      cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B->stage) != cudaSuccess)
+    return HS_ECUDA;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, B->threads, B->stage) != cudaSuccess)
     return HS_ECUDA;
   const int cap = per_sm * B->nsm;
   int grid = 0;
@@ -436,6 +444,7 @@ extern "C" int hs_batch_plan(hs_batch* B, int v, int* grid_out, int* capacity_ou
   if (B->graph) { cudaGraphDestroy(B->graph); B->graph = nullptr; }
   B->grid = grid;
   B->v = v;
+  if (cudaMemcpyToSymbol(c_stage_bytes, &B->stage, sizeof(unsigned)) != cudaSuccess) return HS_ECUDA;
   if (cudaMemcpy(B->d_desc, B->host_desc.data(), sizeof(BatchInst) * B->n, cudaMemcpyHostToDevice) != cudaSuccess)
     return HS_ECUDA;
   return HS_OK;
@@ -458,7 +467,7 @@ extern "C" int hs_batch_run(hs_batch* B, void* stream, hs_batch_result* r) {
     int ni = B->n;
     void* args[] = {&dd, &ni};
     const void* fn = B->mode == HS_MODE_INC ? (const void*)k_batch<M_INC> : (const void*)k_batch<M_REF>;
-    cudaError_t e = cudaLaunchKernel(fn, dim3(B->grid), dim3(B->threads), args, kBatchBuf, cap);
+    cudaError_t e = cudaLaunchKernel(fn, dim3(B->grid), dim3(B->threads), args, B->stage, cap);
     cudaGraph_t g = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(cap, &g);
     cudaStreamDestroy(cap);
@@ -515,6 +524,23 @@ extern "C" int hs_batch_run_serial(hs_batch* B, void* stream, hs_batch_result* r
   r->ops = total_ops(B);
   return read_statuses(B, r);
 }
+
+// Staging bytes per CTA for the bulk-copy critical section (0: the largest
+// instance chunk, i.e. whole-chunk copies).  Invalidates the plan.
+extern "C" int hs_batch_set_stage(hs_batch* B, unsigned bytes) {
+  if (!B) return HS_EINVAL;
+  size_t mx = 1024;
+  for (const auto& c : B->cfg) mx = std::max(mx, (size_t)c.threads * (c.num_ldst + 1) * 4);
+  if (bytes == 0) bytes = (unsigned)mx;
+  bytes = (bytes + 127u) / 128u * 128u;
+  if (bytes > kTmaMaxBytes) { g_berr = "staging buffer above the shared-memory limit"; return HS_EINVAL; }
+  B->stage = bytes;
+  B->grid = 0;
+  if (B->exec) { cudaGraphExecDestroy(B->exec); B->exec = nullptr; }
+  if (B->graph) { cudaGraphDestroy(B->graph); B->graph = nullptr; }
+  return HS_OK;
+}
+extern "C" unsigned hs_batch_get_stage(hs_batch* B) { return B ? B->stage : 0u; }
 
 // Autotuner: try TBs-per-CTA v in {1, 2, 4, ...} whose gangs fit, time one
 // replay each on a copy of the initial storage, keep the fastest plan.

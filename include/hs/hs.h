@@ -158,6 +158,10 @@ int hs_batch_set_storage(hs_batch* b, int i, const uint32_t* host);
 int hs_batch_get_storage(hs_batch* b, int i, uint32_t* host);
 /* Gang plan with v logical TBs per CTA; HS_ENORES if the gangs cannot be co-resident. */
 int hs_batch_plan(hs_batch* b, int v, int* grid, int* capacity);
+/* Staging bytes per CTA for bulk-copy critical sections (0 = the largest chunk:
+ * whole-chunk copies, fewer CTAs per SM).  Default 40 KiB.  Invalidates the plan. */
+int hs_batch_set_stage(hs_batch* b, unsigned bytes);
+unsigned hs_batch_get_stage(hs_batch* b);
 /* Try v = 1, 2, 4, ... and keep the fastest plan that fits (storage is restored after each try). */
 int hs_batch_autotune(hs_batch* b, void* stream, int* best_v, float* best_ms);
 /* Lock-state reset + persistent kernel, captured once per plan into a CUDA graph and replayed. */
