@@ -117,6 +117,8 @@ __device__ __noinline__ bool batch_sem_op(const RunDesc& d, int b, TmaCtx& t, co
       ok = batch_cs<MODE>(d, cur, t, env);
       cur = uniq ? (cur + numSM) % Gd : cur + 1;
     }
+  } else if (d.L > 16) {
+    ok = cs_read_tma_tiled(d, uniq ? b : p, t, c_stage_bytes, env, d.sink + b);
   } else {
     cs_read(d.data + (size_t)(uniq ? b : p) * chunk_words(d.T, d.L), d.T, d.L, d.sink + b);
   }
