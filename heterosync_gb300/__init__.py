@@ -436,6 +436,9 @@ class Batch:
         for f in ("hs_batch_run", "hs_batch_run_serial"):
             getattr(L, f).argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L.hs_batch_plan.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        L.hs_batch_plan_ex.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                       ctypes.c_void_p]
+        L.hs_batch_get_plan.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 4
         L.hs_batch_autotune.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L.hs_batch_destroy.argtypes = [ctypes.c_void_p]
         self.instances = list(instances)
@@ -469,6 +472,21 @@ class Batch:
         grid, cap = ctypes.c_int(), ctypes.c_int()
         s = lib().hs_batch_plan(self.h, v, ctypes.byref(grid), ctypes.byref(cap))
         return s, grid.value, cap.value
+
+    def plan_ex(self, cl: int, serial_execs: int, v: int):
+        """Clusters of cl CTAs per operation; serial_execs clusters for each
+        instance serialised on one lock or semaphore (0 = ceil(numTBs / v)),
+        ceil(numTBs / v) clusters for the others."""
+        grid, cap = ctypes.c_int(), ctypes.c_int()
+        s = lib().hs_batch_plan_ex(self.h, cl, serial_execs, v, ctypes.byref(grid), ctypes.byref(cap))
+        return s, grid.value, cap.value
+
+    def get_plan(self):
+        """(cluster size, serialised-instance clusters, v, grid) of the current plan."""
+        a, b, c, d = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._check(lib().hs_batch_get_plan(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                            ctypes.byref(d)))
+        return a.value, b.value, c.value, d.value
 
     def set_stage(self, nbytes: int):
         """Staging bytes per CTA (0 = whole chunks); invalidates the plan."""

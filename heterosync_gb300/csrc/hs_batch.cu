@@ -44,30 +44,63 @@ struct BatchInst {
   RunDesc d;
   int first_cta;  // first CTA of the gang
   int gang;       // CTAs in the gang
+  int ecl;        // CTAs per executor: 1, or the cluster size (gang aligned to clusters)
+  int index;      // instance number
 };
 
 __device__ __forceinline__ bool is_mutex_prim(int p) { return (p >= 4 && p <= 7) || (p >= 20 && p <= 23); }
 __device__ __forceinline__ bool is_sem_prim(int p) { return (p >= 8 && p <= 15) || (p >= 24 && p <= 31); }
 
-// One critical section of a mutex logical TB b at iteration j.
-// Batch critical section: bulk copies through the CTA's staging buffer (the
-// whole chunk when it fits, else a tile of regions at a time) for numLdSt > 16,
-// vector loads otherwise.  The staging size is a launch parameter the
-// autotuner chooses (a small buffer keeps four CTAs per SM; a whole-chunk
-// buffer moves each chunk with one bulk load).
+// Staging bytes for the bulk-copy critical section (a launch parameter).
 constexpr unsigned kBatchBufSmall = 40u * 1024u;
 __constant__ unsigned c_stage_bytes;
 
+// The cluster's share of one chunk's critical section: rank cr of cl moves
+// regions [cr*R/cl, (cr+1)*R/cl) through its own bulk-copy engine.
 template <int MODE>
-__device__ __forceinline__ bool batch_cs(const RunDesc& d, int chunk, TmaCtx& t, const HsEnv& env) {
-  if (d.L > 16) return cs_chunk_tma_tiled<MODE>(d, chunk, t, c_stage_bytes, env);
-  cs_chunk<MODE, 4>(d, chunk);
-  return true;
+__device__ __forceinline__ bool cl_cs(const RunDesc& d, int chunk, int cr, int cl, TmaCtx& t, const HsEnv& env) {
+  const int R = d.T >> 4;
+  const int lo = cr * R / cl, hi = (cr + 1) * R / cl;
+  if (lo >= hi) return true;
+  if (cl == 1 && d.L <= 16) {
+    cs_chunk<MODE, 4>(d, chunk);
+    return true;
+  }
+  return cs_chunk_tma_tiled<MODE>(d, chunk, t, c_stage_bytes, env, lo, hi);
 }
 
+__device__ __forceinline__ void cl_barrier(int cl) {
+  if (cl > 1) cluster_sync_all();
+}
+
+// End of a cluster operation: every rank has finished its share, and all ranks
+// agree on whether every share succeeded (each rank's flag goes to the leader's
+// s_ok[1 + rank] through distributed shared memory before the barrier).
+__device__ __forceinline__ bool cl_end(int* s_ok, bool cs_ok, int cr, int cl) {
+  if (cl == 1) return cs_ok;
+  if (is_master()) *reinterpret_cast<volatile int*>(map_shared_rank(s_ok + 1 + cr, 0)) = cs_ok ? 1 : 0;
+  cluster_sync_all();
+  const volatile int* f = map_shared_rank(s_ok + 1, 0);
+  bool all = true;
+  for (int i = 0; i < cl; ++i) all = all && f[i] != 0;
+  return all;
+}
+
+// After the leader's wait: every rank learns whether it succeeded (the leader's
+// flag read through distributed shared memory).
+__device__ __forceinline__ bool cl_grant(int* s_ok, int leader_ok, int cr, int cl) {
+  if (cl == 1) return __syncthreads_and(is_master() ? leader_ok : 1) != 0;
+  if (cr == 0 && is_master()) *s_ok = leader_ok;
+  cluster_sync_all();
+  const int* leader = map_shared_rank(s_ok, 0);
+  return *reinterpret_cast<const volatile int*>(leader) != 0;
+}
+
+// One critical section of mutex logical TB b at iteration j, executed by the
+// whole cluster: rank 0 takes and releases the lock, every rank moves its share.
 template <int MODE>
-__device__ __noinline__ bool batch_mutex_op(const RunDesc& d, int b, int j, int* s_slot, TmaCtx& t,
-                                            const HsEnv& env) {
+__device__ __noinline__ bool cl_mutex_op(const RunDesc& d, int b, int cr, int cl, int* s_slot, int* s_ok, TmaCtx& t,
+                                         const HsEnv& env) {
   const bool uniq = d.prim >= 20;
   const int kind = d.prim % 4;  // 0 spin, 1 EBO, 2 ring, 3 ticket (main.cu:1224-1256 order)
   const int g = uniq ? (b % d.nsm) : 0;
@@ -76,32 +109,30 @@ __device__ __noinline__ bool batch_mutex_op(const RunDesc& d, int b, int j, int*
   unsigned* w2 = group_line(d, g, 2);
   unsigned* ring = d.ring + (size_t)g * (d.ring_max + 1) * kRingStride;
   const unsigned wrap = uniq ? 100000000u : 1000000000u;
-  bool ok;
-  int slot = 0;
-  if (kind == 0) ok = spin_lock<GPU>(w0, env);
-  else if (kind == 1) ok = ebo_lock<GPU>(w0, d.bo_min, d.bo_max, env);
-  else if (kind == 3) ok = ticket_lock<GPU>(w0, w1, wrap, d.bo_unit, d.bo_max, env);
-  else {
-    slot = queue_lock<GPU>(w2, ring, kRingStride, d.ring_max, d.bo_unit, env, s_slot);
-    ok = slot >= 0;
+  int ok = 1, slot = 0;
+  if (cr == 0) {
+    if (kind == 0) ok = spin_lock<GPU>(w0, env);
+    else if (kind == 1) ok = ebo_lock<GPU>(w0, d.bo_min, d.bo_max, env);
+    else if (kind == 3) ok = ticket_lock<GPU>(w0, w1, wrap, d.bo_unit, d.bo_max, env);
+    else {
+      slot = queue_lock<GPU>(w2, ring, kRingStride, d.ring_max, d.bo_unit, env, s_slot);
+      ok = slot >= 0;
+    }
   }
-  if (!ok) return false;
-  bool cs_ok = true;
-  if (MODE == M_SLICE) {
-    const int G = uniq ? d.nsm : 1, r = b / G, m = (d.num_tbs - g + G - 1) / G;
-    cs_slice(d.data, g + ((r + j) % m) * G, d.L);
-  } else {
-    cs_ok = batch_cs<MODE>(d, g, t, env);
+  if (!cl_grant(s_ok, ok, cr, cl)) return false;
+  const bool cs_ok = cl_end(s_ok, cl_cs<MODE>(d, g, cr, cl, t, env), cr, cl);
+  if (cr == 0) {
+    if (kind <= 1) spin_unlock<GPU>(w0);
+    else if (kind == 3) ticket_unlock<GPU>(w1, wrap);
+    else queue_unlock<GPU>(ring, kRingStride, d.ring_max, (unsigned)slot);
   }
-  if (kind <= 1) spin_unlock<GPU>(w0);
-  else if (kind == 3) ticket_unlock<GPU>(w1, wrap);
-  else queue_unlock<GPU>(ring, kRingStride, d.ring_max, (unsigned)slot);
   return cs_ok;
 }
 
-// One wait/CS/post of a semaphore logical TB b.
+// One wait/CS/post of semaphore logical TB b, executed by the whole cluster.
 template <int MODE>
-__device__ __noinline__ bool batch_sem_op(const RunDesc& d, int b, TmaCtx& t, const HsEnv& env) {
+__device__ __noinline__ bool cl_sem_op(const RunDesc& d, int b, int cr, int cl, int* s_ok, TmaCtx& t,
+                                       const HsEnv& env) {
   const bool uniq = d.prim >= 24;
   const bool ebo = (d.prim >= 12 && d.prim <= 15) || d.prim >= 28;
   const int Gd = d.num_tbs;
@@ -109,21 +140,25 @@ __device__ __noinline__ bool batch_sem_op(const RunDesc& d, int b, TmaCtx& t, co
   const int smID = b % numSM, k = ceil_div(Gd, numSM), p = b / numSM;
   const bool writer = (p == smID % k);
   unsigned* st = group_line(d, uniq ? smID : 0, 0);
-  if (!sem_wait<GPU>(st, writer, d.sem_max, ebo, !uniq, d.bo_min, d.bo_max, env)) return false;
-  bool ok = true;
+  int ok = 1;
+  if (cr == 0) ok = sem_wait<GPU>(st, writer, d.sem_max, ebo, !uniq, d.bo_min, d.bo_max, env);
+  if (!cl_grant(s_ok, ok, cr, cl)) return false;
+  bool cs_ok = true;
   if (writer) {
     int cur = uniq ? b : 0;
-    for (int j = 0; j < k && ok; ++j) {
-      ok = batch_cs<MODE>(d, cur, t, env);
+    for (int j = 0; j < k && cs_ok; ++j) {
+      cs_ok = cl_cs<MODE>(d, cur, cr, cl, t, env);
       cur = uniq ? (cur + numSM) % Gd : cur + 1;
     }
-  } else if (d.L > 16) {
-    ok = cs_read_tma_tiled(d, uniq ? b : p, t, c_stage_bytes, env, d.sink + b);
   } else {
-    cs_read(d.data + (size_t)(uniq ? b : p) * chunk_words(d.T, d.L), d.T, d.L, d.sink + b);
+    const int R = d.T >> 4, lo = cr * R / cl, hi = (cr + 1) * R / cl;
+    const int rc = uniq ? b : p;
+    if (cl == 1 && d.L <= 16) cs_read(d.data + (size_t)rc * chunk_words(d.T, d.L), d.T, d.L, d.sink + b);
+    else if (lo < hi) cs_ok = cs_read_tma_tiled(d, rc, t, c_stage_bytes, env, d.sink + b, lo, hi);
   }
-  sem_post<GPU>(st, writer, d.sem_max);
-  return ok;
+  cs_ok = cl_end(s_ok, cs_ok, cr, cl);
+  if (cr == 0) sem_post<GPU>(st, writer, d.sem_max);
+  return cs_ok;
 }
 
 // Counter barrier among the gang's CTAs (instance's global barrier lines).
@@ -141,7 +176,8 @@ __device__ __forceinline__ bool gang_barrier(const RunDesc& d, unsigned n, unsig
 
 // Tree-barrier instance: every logical TB's chunk once per phase, a gang
 // barrier after each phase (LocalExch: a second phase on the chunk
-// numBlocksAtBarr TBs ahead, main.cu:153-211).
+// numBlocksAtBarr TBs ahead, main.cu:153-211).  Each gang CTA handles the
+// logical TBs congruent to its rank.
 template <int MODE>
 __device__ __noinline__ void batch_barrier(const RunDesc& d, int rank, int c, unsigned gen, TmaCtx& t,
                                            const HsEnv& env) {
@@ -150,11 +186,11 @@ __device__ __noinline__ void batch_barrier(const RunDesc& d, int rank, int c, un
   for (int e = 0; e < d.iters; ++e) {
     const long long base = exch ? (long long)e * (nb + 1) : (long long)e;
     for (int b = rank; b < G; b += c)
-      if (!batch_cs<MODE>(d, (int)((b + base) % G), t, env)) return;
+      if (!cl_cs<MODE>(d, (int)((b + base) % G), 0, 1, t, env)) return;
     if (!gang_barrier(d, (unsigned)c, gen, env)) return;
     if (exch) {
       for (int b = rank; b < G; b += c)
-        if (!batch_cs<MODE>(d, (int)((b + base + nb) % G), t, env)) return;
+        if (!cl_cs<MODE>(d, (int)((b + base + nb) % G), 0, 1, t, env)) return;
       if (!gang_barrier(d, (unsigned)c, gen, env)) return;
     }
   }
@@ -164,12 +200,15 @@ template <int MODE>
 __global__ void __launch_bounds__(256, 4) k_batch(const BatchInst* insts, int n_inst) {
   __shared__ int s_slot;
   __shared__ int s_inst;
+  __shared__ int s_ok[9];  // [0] grant, [1 + rank] share succeeded
   __shared__ unsigned s_gen;
   __shared__ unsigned long long s_mbar;
   extern __shared__ __align__(128) unsigned char dyn_smem[];
   TmaCtx tma;
   tma_init(tma, &s_mbar, dyn_smem);
   const int cta = blockIdx.x;
+  const int cl = (int)cluster_nctarank();
+  const int cr = (int)cluster_ctarank();
   if (is_master()) {  // gang lookup: binary search over first_cta
     int lo = 0, hi = n_inst - 1;
     while (lo < hi) {
@@ -184,19 +223,25 @@ __global__ void __launch_bounds__(256, 4) k_batch(const BatchInst* insts, int n_
   const BatchInst& bi = insts[s_inst];
   const RunDesc d = bi.d;
   const int rank = cta - bi.first_cta, c = bi.gang;
-  if (rank < 0 || rank >= c) return;
   const HsEnv env{d.status, d.timeout_ns};
-  if (is_mutex_prim(d.prim)) {
-    for (int j = 0; j < d.iters; ++j)
-      for (int b = rank; b < d.num_tbs; b += c)
-        if (!batch_mutex_op<MODE>(d, b, j, &s_slot, tma, env)) return;
-  } else if (is_sem_prim(d.prim)) {
-    for (int j = 0; j < d.iters; ++j)
-      for (int b = rank; b < d.num_tbs; b += c)
-        if (!batch_sem_op<MODE>(d, b, tma, env)) return;
-  } else {
-    batch_barrier<MODE>(d, rank, c, s_gen, tma, env);
+  if (rank >= 0 && rank < c) {
+    if (is_mutex_prim(d.prim) || is_sem_prim(d.prim)) {
+      // one executor per ecl CTAs (a whole cluster, or one CTA); executor x
+      // runs the logical TBs congruent to x
+      const int ecl = bi.ecl, er = ecl == 1 ? 0 : cr;
+      const int execs = c / ecl, x = rank / ecl;
+      const bool mtx = is_mutex_prim(d.prim);
+      bool ok = true;
+      for (int j = 0; j < d.iters && ok; ++j)
+        for (int b = x; b < d.num_tbs && ok; b += execs)
+          ok = mtx ? cl_mutex_op<MODE>(d, b, er, ecl, &s_slot, s_ok, tma, env)
+                   : cl_sem_op<MODE>(d, b, er, ecl, s_ok, tma, env);
+    } else {
+      batch_barrier<MODE>(d, rank, c, s_gen, tma, env);
+    }
   }
+  // no CTA of a cluster may exit while another rank can still read its shared memory
+  cl_barrier(cl);
 }
 
 }  // namespace hs
@@ -212,7 +257,8 @@ struct hs_batch {
   std::vector<hs_run_config> cfg;
   std::vector<size_t> words;
   std::vector<Layout> lay;
-  std::vector<BatchInst> host_desc;
+  std::vector<BatchInst> host_desc;  // by instance
+  std::vector<BatchInst> dev_order;  // by first CTA (the device copy)
   unsigned* storage = nullptr;   // all instances' storage, 256-byte aligned slices
   std::vector<size_t> st_off;    // word offsets
   unsigned* state = nullptr;     // all lock state, rings, sinks, status
@@ -223,6 +269,7 @@ struct hs_batch {
   cudaGraphExec_t exec = nullptr;
   unsigned graph_kernels = 0;
   unsigned stage = kBatchBufSmall;  // staging bytes per CTA
+  int cl = 1, serial_execs = 0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
 };
 
@@ -344,6 +391,8 @@ extern "C" int hs_batch_create(const hs_batch_instance* inst, int n, int threads
     bi.d = d;
     bi.first_cta = 0;
     bi.gang = 1;
+    bi.ecl = 1;
+    bi.index = i;
     B->host_desc.push_back(bi);
   }
   cudaEventCreate(&B->e0);
@@ -419,23 +468,78 @@ static unsigned long long total_ops(const hs_batch* B) {
   return o;
 }
 
-// Gangs of ceil(numTBs / v) CTAs.  Returns the grid size, or 0 if it cannot be co-resident.
-extern "C" int hs_batch_plan(hs_batch* B, int v, int* grid_out, int* capacity_out) {
-  if (!B || v <= 0) return HS_EINVAL;
-  int per_sm = 0;
+// Gang plan.  cl: thread-block cluster size of the launch; serial_execs:
+// executors of the heaviest instance whose operations serialise on one lock or
+// semaphore (global mutexes and semaphores; 0 = ceil(numTBs / v) for each);
+// v: logical TBs per executor for the other instances (per-SM locks and
+// semaphores, barriers).  Returns HS_ENORES if the gangs cannot be co-resident.
+static bool serialized_prim(int p) { return p >= 4 && p <= 15; }
+static double cs_work(const hs_run_config& c) { return (double)c.num_tbs * c.num_iters * (c.num_ldst + 1); }
+// Below this many loads/stores per thread the two cluster barriers of an
+// operation cost more than splitting its critical section saves.
+constexpr int kClusterMinLdSt = 33;
+
+extern "C" int hs_batch_plan_ex(hs_batch* B, int cl, int serial_execs, int v, int* grid_out, int* capacity_out) {
+  if (!B || v <= 0 || cl < 1 || cl > 8 || (cl & (cl - 1))) return HS_EINVAL;
   auto fn = B->mode == HS_MODE_INC ? k_batch<M_INC> : k_batch<M_REF>;
   if (B->stage > 48u * 1024u &&
       cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B->stage) != cudaSuccess)
     return HS_ECUDA;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, B->threads, B->stage) != cudaSuccess)
-    return HS_ECUDA;
-  const int cap = per_sm * B->nsm;
-  int grid = 0;
-  for (int i = 0; i < B->n; ++i) {
-    B->host_desc[i].first_cta = grid;
-    B->host_desc[i].gang = (B->cfg[i].num_tbs + v - 1) / v;
-    grid += B->host_desc[i].gang;
+  int cap = 0;
+  if (cl == 1) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, B->threads, B->stage) != cudaSuccess)
+      return HS_ECUDA;
+    cap = per_sm * B->nsm;
+  } else {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)cl;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)(cl * 64));
+    cfg.blockDim = dim3((unsigned)B->threads);
+    cfg.dynamicSmemBytes = B->stage;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, (const void*)fn, &cfg) != cudaSuccess) {
+      cudaGetLastError();
+      return HS_ECUDA;
+    }
+    cap = clusters * cl;
   }
+  // Serialised instances share serial_execs executors in proportion to their
+  // critical-section work numTBs * numCSIters * (numLdSt + 1) (the heaviest
+  // gets serial_execs); those with numLdSt >= kClusterMinLdSt execute as whole
+  // clusters.  Cluster-executed gangs are placed first (aligned), one-CTA
+  // executors after them, packed.
+  double wmax = 0.0;
+  for (int i = 0; i < B->n; ++i)
+    if (serialized_prim(B->cfg[i].prim)) wmax = std::max(wmax, cs_work(B->cfg[i]));
+  std::vector<int> execs(B->n), ecl(B->n);
+  for (int i = 0; i < B->n; ++i) {
+    const hs_run_config& c = B->cfg[i];
+    const int G = c.num_tbs;
+    int e = (G + v - 1) / v;
+    ecl[i] = 1;
+    if (serialized_prim(c.prim)) {
+      if (serial_execs > 0) e = (int)std::lround(serial_execs * cs_work(c) / wmax);
+      if (cl > 1 && c.num_ldst >= kClusterMinLdSt) ecl[i] = cl;
+    }
+    execs[i] = std::max(1, std::min(G, e));
+  }
+  int grid = 0;
+  for (int pass = 0; pass < 2; ++pass)
+    for (int i = 0; i < B->n; ++i) {
+      if ((ecl[i] > 1) != (pass == 0)) continue;
+      B->host_desc[i].first_cta = grid;
+      B->host_desc[i].gang = execs[i] * ecl[i];
+      B->host_desc[i].ecl = ecl[i];
+      grid += execs[i] * ecl[i];
+    }
+  grid = (grid + cl - 1) / cl * cl;  // the tail's idle CTAs complete the last cluster
   if (capacity_out) *capacity_out = cap;
   if (grid_out) *grid_out = grid;
   if (grid > cap) {
@@ -446,10 +550,20 @@ extern "C" int hs_batch_plan(hs_batch* B, int v, int* grid_out, int* capacity_ou
   if (B->graph) { cudaGraphDestroy(B->graph); B->graph = nullptr; }
   B->grid = grid;
   B->v = v;
+  B->cl = cl;
+  B->serial_execs = serial_execs;
   if (cudaMemcpyToSymbol(c_stage_bytes, &B->stage, sizeof(unsigned)) != cudaSuccess) return HS_ECUDA;
-  if (cudaMemcpy(B->d_desc, B->host_desc.data(), sizeof(BatchInst) * B->n, cudaMemcpyHostToDevice) != cudaSuccess)
+  B->dev_order = B->host_desc;
+  std::sort(B->dev_order.begin(), B->dev_order.end(),
+            [](const BatchInst& x, const BatchInst& y) { return x.first_cta < y.first_cta; });
+  if (cudaMemcpy(B->d_desc, B->dev_order.data(), sizeof(BatchInst) * B->n, cudaMemcpyHostToDevice) != cudaSuccess)
     return HS_ECUDA;
   return HS_OK;
+}
+
+// Gangs of ceil(numTBs / v) CTAs, no clusters.
+extern "C" int hs_batch_plan(hs_batch* B, int v, int* grid_out, int* capacity_out) {
+  return hs_batch_plan_ex(B, 1, 0, v, grid_out, capacity_out);
 }
 
 // Capture (once per plan) and replay: lock-state reset + the persistent kernel.
@@ -469,7 +583,19 @@ extern "C" int hs_batch_run(hs_batch* B, void* stream, hs_batch_result* r) {
     int ni = B->n;
     void* args[] = {&dd, &ni};
     const void* fn = B->mode == HS_MODE_INC ? (const void*)k_batch<M_INC> : (const void*)k_batch<M_REF>;
-    cudaError_t e = cudaLaunchKernel(fn, dim3(B->grid), dim3(B->threads), args, B->stage, cap);
+    cudaLaunchConfig_t lc = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)B->cl;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    lc.gridDim = dim3((unsigned)B->grid);
+    lc.blockDim = dim3((unsigned)B->threads);
+    lc.dynamicSmemBytes = B->stage;
+    lc.stream = cap;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelExC(&lc, fn, args);
     cudaGraph_t g = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(cap, &g);
     cudaStreamDestroy(cap);
@@ -544,8 +670,9 @@ extern "C" int hs_batch_set_stage(hs_batch* B, unsigned bytes) {
 }
 extern "C" unsigned hs_batch_get_stage(hs_batch* B) { return B ? B->stage : 0u; }
 
-// Autotuner: try TBs-per-CTA v in {1, 2, 4, ...} whose gangs fit, time one
-// replay each on a copy of the initial storage, keep the fastest plan.
+// Autotuner: for cluster sizes 1, 4, 8 and 4 to 32 executors for the heaviest
+// serialised instance, take the smallest v (1, 2, 4, ...) whose gangs fit, time
+// one replay on a copy of the initial storage, and keep the fastest plan.
 extern "C" int hs_batch_autotune(hs_batch* B, void* stream, int* best_v, float* best_ms) {
   if (!B) return HS_EINVAL;
   std::vector<std::vector<uint32_t>> saved(B->n);
@@ -553,21 +680,34 @@ extern "C" int hs_batch_autotune(hs_batch* B, void* stream, int* best_v, float* 
     saved[i].resize(B->words[i]);
     hs_batch_get_storage(B, i, saved[i].data());
   }
-  int best = 0;
-  float best_t = 1e30f;
   int max_g = 1;
   for (const auto& c : B->cfg) max_g = std::max(max_g, c.num_tbs);
-  for (int v = 1; v <= max_g * 2; v *= 2) {
-    int grid = 0, cap = 0;
-    if (hs_batch_plan(B, v, &grid, &cap) != HS_OK) continue;
-    hs_batch_result r;
-    if (hs_batch_run(B, stream, &r) != HS_OK) continue;
-    if (r.elapsed_ms < best_t) { best_t = r.elapsed_ms; best = v; }
-    for (int i = 0; i < B->n; ++i) hs_batch_set_storage(B, i, saved[i].data());
+  float best_t = 1e30f;
+  int bcl = 0, bse = 0, bv = 0;
+  for (int cl : {1, 4, 8}) {
+    for (int se : {4, 8, 16, 32}) {
+      int v = 1;
+      while (v <= max_g && hs_batch_plan_ex(B, cl, se, v, nullptr, nullptr) != HS_OK) v *= 2;
+      if (v > max_g) continue;
+      hs_batch_result r;
+      const int s = hs_batch_run(B, stream, &r);
+      for (int i = 0; i < B->n; ++i) hs_batch_set_storage(B, i, saved[i].data());
+      if (s != HS_OK) continue;
+      if (r.elapsed_ms < best_t) { best_t = r.elapsed_ms; bcl = cl; bse = se; bv = v; }
+    }
   }
-  if (!best) { g_berr = "no plan fits"; return HS_ENORES; }
-  hs_batch_plan(B, best, nullptr, nullptr);
-  if (best_v) *best_v = best;
+  if (!bcl) { g_berr = "no plan fits"; return HS_ENORES; }
+  hs_batch_plan_ex(B, bcl, bse, bv, nullptr, nullptr);
+  if (best_v) *best_v = bv;
   if (best_ms) *best_ms = best_t;
+  return HS_OK;
+}
+
+extern "C" int hs_batch_get_plan(hs_batch* B, int* cl, int* serial_execs, int* v, int* grid) {
+  if (!B) return HS_EINVAL;
+  if (cl) *cl = B->cl;
+  if (serial_execs) *serial_execs = B->serial_execs;
+  if (v) *v = B->v;
+  if (grid) *grid = B->grid;
   return HS_OK;
 }

@@ -225,14 +225,14 @@ __device__ __forceinline__ bool cs_chunk_tma(const RunDesc& d, int chunk, TmaCtx
 // it (wait_group.read).
 template <int MODE>
 __device__ __forceinline__ bool cs_chunk_tma_tiled(const RunDesc& d, int chunk, TmaCtx& t, unsigned buf_bytes,
-                                                   const HsEnv& env) {
+                                                   const HsEnv& env, int r_lo = 0, int r_hi = -1) {
   unsigned* c = d.data + (size_t)chunk * chunk_words(d.T, d.L);
-  const int R = d.T >> 4;
+  const int R = r_hi < 0 ? (d.T >> 4) : r_hi;
   const unsigned rb = (unsigned)(64 * (d.L + 1));
   int per = (int)(buf_bytes / rb);
   if (per < 1) per = 1;
   const unsigned sbase = smem_addr(t.buf);
-  for (int r0 = 0; r0 < R; r0 += per) {
+  for (int r0 = r_lo; r0 < R; r0 += per) {
     const int n = (R - r0 < per) ? (R - r0) : per;
     unsigned char* src = reinterpret_cast<unsigned char*>(c) + (size_t)r0 * rb;
     if (!tma_load_chunk(reinterpret_cast<const unsigned*>(src), (unsigned)n * rb, t, env)) return false;
@@ -269,15 +269,15 @@ __device__ __forceinline__ bool cs_chunk_tma_tiled(const RunDesc& d, int chunk, 
 
 // Semaphore reader through the staging buffer, a tile of regions at a time.
 __device__ __forceinline__ bool cs_read_tma_tiled(const RunDesc& d, int chunk, TmaCtx& t, unsigned buf_bytes,
-                                                  const HsEnv& env, unsigned* sink_slot) {
+                                                  const HsEnv& env, unsigned* sink_slot, int r_lo = 0, int r_hi = -1) {
   const unsigned* c = d.data + (size_t)chunk * chunk_words(d.T, d.L);
-  const int R = d.T >> 4;
+  const int R = r_hi < 0 ? (d.T >> 4) : r_hi;
   const unsigned rb = (unsigned)(64 * (d.L + 1));
   int per = (int)(buf_bytes / rb);
   if (per < 1) per = 1;
   const int per_region = d.L * 4, rw4 = (d.L + 1) * 4;
   unsigned acc = 0;
-  for (int r0 = 0; r0 < R; r0 += per) {
+  for (int r0 = r_lo; r0 < R; r0 += per) {
     const int n = (R - r0 < per) ? (R - r0) : per;
     if (!tma_load_chunk(c + (size_t)r0 * (rb / 4), (unsigned)n * rb, t, env)) return false;
     const uint4* s4 = reinterpret_cast<const uint4*>(t.buf);

@@ -158,6 +158,15 @@ int hs_batch_set_storage(hs_batch* b, int i, const uint32_t* host);
 int hs_batch_get_storage(hs_batch* b, int i, uint32_t* host);
 /* Gang plan with v logical TBs per CTA; HS_ENORES if the gangs cannot be co-resident. */
 int hs_batch_plan(hs_batch* b, int v, int* grid, int* capacity);
+/* General plan, launched with thread-block clusters of cl CTAs (1, 2, 4 or 8).
+ * Instances whose operations serialise on one lock or semaphore (global mutexes
+ * and semaphores) get executors in proportion to numTBs * numCSIters *
+ * (numLdSt + 1), serial_execs for the heaviest (0 = ceil(numTBs / v) each); with
+ * numLdSt >= 33 each executor is a whole cluster (the holder's critical section
+ * split over its SMs), else one CTA.  The other instances get ceil(numTBs / v)
+ * one-CTA executors. */
+int hs_batch_plan_ex(hs_batch* b, int cl, int serial_execs, int v, int* grid, int* capacity);
+int hs_batch_get_plan(hs_batch* b, int* cl, int* serial_execs, int* v, int* grid);
 /* Staging bytes per CTA for bulk-copy critical sections (0 = the largest chunk:
  * whole-chunk copies, fewer CTAs per SM).  Default 40 KiB.  Invalidates the plan. */
 int hs_batch_set_stage(hs_batch* b, unsigned bytes);

@@ -60,3 +60,28 @@ def test_plan_rejects_non_co_resident_gangs(hs):
     s, grid, cap = b.plan(1)
     assert grid == 4096 and (s == 3) == (grid > cap)
     b.close()
+
+
+@pytest.mark.parametrize("cl", [2, 4, 8])
+@pytest.mark.parametrize("mode", ["inc", "ref"])
+def test_cluster_plans_bit_exact(hs, cl, mode):
+    """Clusters of cl CTAs execute each mutex/semaphore operation together (the
+    leader holds the lock, every rank moves a slice of the regions)."""
+    insts = [(p, 5 + (p % 7) * 13, 2 + p % 11, 3 + p % 3) for p in
+             [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30, 31]]
+    b = hs.Batch(insts, mode=mode)
+    rng = np.random.default_rng(11 + cl)
+    inits = [rng.integers(0, 2**32, size=b.words(i), dtype=np.uint64).astype(np.uint32) for i in range(len(insts))]
+    for se in (1, 2, 0):
+        s, grid, cap = b.plan_ex(cl, se, 1)
+        if s == 3:
+            continue
+        assert s == 0 and grid % cl == 0
+        assert b.get_plan()[:3] == (cl, se, 1)
+        for i, a in enumerate(inits):
+            b.set_storage(i, a)
+        r = b.run()
+        assert r.dev_error_bits == 0
+        for i, a in enumerate(inits):
+            assert np.array_equal(b.get_storage(i), _expected(hs, insts[i], a, mode)), (cl, se, i, insts[i])
+    b.close()
