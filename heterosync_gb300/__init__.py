@@ -399,6 +399,47 @@ def uts_run(tree, frontier, host_processed: int, blocks: int, threads: int = 128
 
 
 # ---------------------------------------------------------------------------
+# Tree barrier with local exchange on thread-block clusters (hs_exchange_*)
+# ---------------------------------------------------------------------------
+class _ExchResult(ctypes.Structure):
+    _fields_ = [("elapsed_ms", ctypes.c_float), ("episodes_per_s", ctypes.c_double),
+                ("exchange_gbs", ctypes.c_double), ("clusters", ctypes.c_int), ("dev_error_bits", ctypes.c_uint),
+                ("wait_site", ctypes.c_uint)]
+
+
+def exchange_fill(seed: int, n: int, elems: int):
+    """(n, elems) uint32 words holding fp32 values uniform in [-1, 1) drawn
+    from std::mt19937_64(seed)."""
+    np = _np()
+    out = np.empty((n, elems), dtype=np.uint32)
+    lib().hs_exchange_fill.argtypes = [ctypes.c_ulonglong, ctypes.c_size_t, ctypes.c_void_p]
+    s = lib().hs_exchange_fill(seed, out.size, _p(out))
+    if s:
+        raise HsError(s, "exchange fill")
+    return out
+
+
+def exchange_run(buffers, cluster: int, lf: bool, episodes: int, timeout_ns: int = 0):
+    """Rotate the (n, elems) buffers by `episodes` CTAs, one tree barrier per
+    episode, clusters of `cluster` CTAs.  Returns (final buffers, result)."""
+    np = _np()
+    buffers = np.ascontiguousarray(buffers, dtype=np.uint32)
+    if buffers.ndim != 2:
+        raise ValueError("buffers must be (n, elems)")
+    out = np.empty_like(buffers)
+    r = _ExchResult()
+    L = lib()
+    L.hs_exchange_last_error.restype = ctypes.c_char_p
+    L.hs_exchange_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                  ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong, ctypes.c_void_p]
+    s = L.hs_exchange_run(_p(buffers), _p(out), buffers.shape[0], buffers.shape[1], cluster, 1 if lf else 0,
+                          episodes, timeout_ns, ctypes.byref(r))
+    if s:
+        raise HsError(s, L.hs_exchange_last_error().decode())
+    return out, r
+
+
+# ---------------------------------------------------------------------------
 # Batched mixed instances (hs_batch_*)
 # ---------------------------------------------------------------------------
 class _BatchInst(ctypes.Structure):

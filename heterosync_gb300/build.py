@@ -38,6 +38,7 @@ CU_SOURCES = [
     "hs_relaxed_api.cu",
     "hs_uts.cu",
     "hs_batch.cu",
+    "hs_exchange.cu",
 ]
 # command-line programs: (output name, source)
 PROGRAMS = [

@@ -225,6 +225,29 @@ int hs_uts_frontier(const hs_uts_node* tree, int num_nodes, int cores_used, int*
 int hs_uts_run(const hs_uts_node* tree, int num_nodes, const int* frontier, int n_frontier, unsigned host_processed,
                int blocks, int threads, unsigned long long timeout_ns, hs_uts_result* out);
 
+/* ---- tree barrier with local exchange on thread-block clusters ----------------- */
+/* The LocalExch tree barriers (main.cu:153-270; joinBarrier_helper,
+ * cudaLocksBarrierAtomic.cu:147-172; joinLFBarrier_helper,
+ * cudaLocksBarrierFast.cu:315-330) with the local level on clusters of
+ * `cluster` CTAs (1, 2, 4, 8): n resident CTAs each own `elems` words; each of
+ * `episodes` episodes rotates every CTA's buffer to CTA (b + 1) mod n through
+ * distributed shared memory (within a cluster) or an L2 staging slot (between
+ * clusters) and ends with one tree barrier (lf = 0: generation counter among the
+ * cluster leaders; lf = 1: per-cluster flags scanned by a master CTA).  host_out
+ * receives the final buffers: host_in rotated by `episodes` CTAs. */
+typedef struct hs_exchange_result {
+  float elapsed_ms;          /* kernel time (CUDA events) */
+  double episodes_per_s;
+  double exchange_gbs;       /* 2 * n * elems * 4 bytes per episode / time */
+  int clusters;
+  unsigned dev_error_bits, wait_site;
+} hs_exchange_result;
+const char* hs_exchange_last_error(void);
+/* words uniform fp32 in [-1, 1): (int32)(r >> 40) * 2^-23 - 1 over std::mt19937_64(seed) draws r. */
+int hs_exchange_fill(unsigned long long seed, size_t words, uint32_t* out);
+int hs_exchange_run(const uint32_t* host_in, uint32_t* host_out, int n, int elems, int cluster, int lf, int episodes,
+                    unsigned long long timeout_ns, hs_exchange_result* r);
+
 /* ---- roofline probes --------------------------------------------------------- */
 /* Aggregate L2 atomic rate: blocks x threads threads each issue `iters`
  * red.add to their own 128-byte-spaced word (same_address = 0: contention-free

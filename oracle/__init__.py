@@ -163,3 +163,12 @@ def uts_frontier(tree, cores_used: int):
     if rc:
         raise ValueError("frontier cannot be filled")
     return fr[:cnt.value].copy(), proc.value
+
+
+def exchange_expected(buffers: np.ndarray, episodes: int) -> np.ndarray:
+    """Tree barrier with local exchange: each episode moves CTA b's buffer to
+    CTA (b + 1) mod n (the exchange phase of main.cu:153-270 works on the data
+    of another TB between two barriers), so after `episodes` episodes CTA b
+    holds the initial buffer of CTA (b - episodes) mod n."""
+    n = buffers.shape[0]
+    return np.roll(buffers, episodes % n if n else 0, axis=0)
