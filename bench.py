@@ -17,6 +17,12 @@ the 6 points, so the default 6 timed steps cover the sweep once.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
+Beside the sweep, outside its timed region, the line carries "exchange" (tree
+barrier with local exchange on thread-block clusters: 592 CTAs, fp32[4096] per
+CTA rotated every episode, 1000 episodes, cluster sizes 1/2/4/8) and "batch"
+(the 64-instance mixed batch, one launch per instance against the autotuned
+persistent graph-replayed launch); --no-extras skips both.
+
 --impl reference runs the reference's own SyncPrims kernels (built from its
 unmodified sources into oracle/_ref) on the same GPU with the same sizes, each
 step a bounded sample (fewer iterations); without oracle/_ref it falls back to
@@ -223,6 +229,68 @@ def cs_bytes(name, G, L, nsm):
     return G * ITERS * T * L * 8
 
 
+def exchange_extra(hs):
+    """Tree barrier with local exchange on clusters: 592 resident CTAs x 256
+    threads, a 4096-word fp32 buffer per CTA rotated to the next CTA every
+    episode, 1000 episodes; cluster sizes 1 (flat), 2, 4, 8, both global stages;
+    final buffers checked bit-exact against the rotation."""
+    import oracle
+    x = hs.exchange_fill(SEED, 592, 4096)
+    rows = {}
+    for lf in (False, True):
+        for cl in (1, 2, 4, 8):
+            out, r = hs.exchange_run(x, cl, lf, 1000)
+            if not np.array_equal(out, oracle.exchange_expected(x, 1000)):
+                raise SystemExit("bench: exchange cluster=%d lf=%s is not the expected rotation" % (cl, lf))
+            rows["%s_cluster%d" % ("lf" if lf else "atomic", cl)] = {
+                "episodes_per_s": round(r.episodes_per_s), "exchange_gbs": round(r.exchange_gbs, 1),
+                "ms": round(r.elapsed_ms, 3)}
+    return {"workload": "592 CTAs x 256 threads, fp32[4096] per CTA rotated to CTA b+1 each episode, "
+                        "1000 episodes, one tree barrier per episode (bit-exact rotation checked)",
+            "exchange_bytes_per_episode": 592 * 4096 * 4 * 2, "results": rows}
+
+
+def batch_extra(hs):
+    """The 64-instance mixed batch (numTBs log-uniform [4,512], numLdSt [1,128],
+    numCSIters [10,5000]): one launch per instance against one persistent
+    graph-replayed launch, plan chosen by the autotuner on the same batch with
+    numCSIters / 25; every instance checked bit-exact after both."""
+    insts = hs.batch_generate(seed=SEED, n=64, iter_div=1)
+    small = hs.batch_generate(seed=SEED, n=64, iter_div=25)
+    tb = hs.Batch(small, mode="inc")
+    _, tune_ms = tb.autotune()
+    cl, se, v, _ = tb.get_plan()
+    tb.close()
+    b = hs.Batch(insts, mode="inc")
+    rng = np.random.default_rng(SEED)
+    inits = [rng.integers(0, 1000, size=b.words(i)).astype(np.uint32) for i in range(len(insts))]
+
+    def check(tag):
+        for i, (p, L, G, I) in enumerate(insts):
+            cfg = hs.RunConfig(prim=p, num_ldst=L, num_tbs=G, num_iters=I, threads=THREADS, repeats=1, mode="inc")
+            if not np.array_equal(b.get_storage(i), hs.expected_storage(cfg, inits[i])):
+                raise SystemExit("bench: batch instance %d differs after the %s run" % (i, tag))
+
+    for i, a in enumerate(inits):
+        b.set_storage(i, a)
+    rs = b.run_serial()
+    check("per-launch")
+    s, grid, cap = b.plan_ex(cl, se, v)
+    if s:
+        raise SystemExit("bench: the tuned batch plan does not fit (status %d)" % s)
+    for i, a in enumerate(inits):
+        b.set_storage(i, a)
+    rb = b.run()
+    check("batched")
+    b.close()
+    return {"workload": "64 mixed SyncPrims instances (seed %d), numCSIters [10,5000]" % SEED,
+            "ops": rb.ops, "per_launch_ms": round(rs.elapsed_ms, 2), "per_launch_ops_per_s": rs.ops / (rs.elapsed_ms * 1e-3),
+            "launches_per_instance_form": rs.launches, "batched_ms": round(rb.elapsed_ms, 2),
+            "batched_ops_per_s": rb.ops / (rb.elapsed_ms * 1e-3), "ratio": rs.elapsed_ms / rb.elapsed_ms,
+            "plan": {"cluster": cl, "serial_executors": se, "tbs_per_executor": v, "grid": grid, "capacity": cap,
+                     "tuned_on": "numCSIters / 25 (%.1f ms)" % tune_ms}}
+
+
 def reference_arm(args, rank):
     import oracle
     hs_nsm = None
@@ -299,6 +367,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-check", action="store_true", help="skip the bit-exact check of every run")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the cluster exchange and mixed-batch figures reported beside the sweep")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -413,6 +483,14 @@ def main():
         }
         if ck:
             out["clocks"] = ck
+        if not args.no_extras and world == 1:
+            for key, fn in (("exchange", exchange_extra), ("batch", batch_extra)):
+                try:
+                    out[key] = fn(hs)
+                except SystemExit:
+                    raise
+                except Exception as e:  # noqa: BLE001
+                    out[key] = {"error": str(e)}
         if not args.no_cpu_baseline and world == 1:
             try:
                 out["cpu_baseline"] = cpu_baseline(nsm)

@@ -1,0 +1,92 @@
+"""Command line for the workloads beside the drop-in programs.
+
+  python -m heterosync_gb300.cli exchange [--ctas 592] [--elems 4096]
+         [--cluster 8] [--lf] [--episodes 1000] [--seed 20260101]
+      tree barrier with local exchange on thread-block clusters; prints one
+      JSON line (episodes/s, exchange GB/s, bit-exact check of the rotation)
+
+  python -m heterosync_gb300.cli batch [--seed 20260101] [--n 64]
+         [--iter-div 1] [--tune-div 25]
+      the mixed-instance batch: one launch per instance, then the autotuned
+      persistent graph-replayed launch; prints one JSON line (both times, the
+      ratio, the plan, bit-exact check of every instance)
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import sys
+
+import numpy as np
+
+from . import (Batch, RunConfig, batch_generate, exchange_fill, exchange_run, expected_storage)
+
+
+def _rotation(x, episodes):
+    return np.roll(x, episodes % x.shape[0], axis=0)
+
+
+def cmd_exchange(a):
+    x = exchange_fill(a.seed, a.ctas, a.elems)
+    out, r = exchange_run(x, a.cluster, a.lf, a.episodes)
+    exact = bool(np.array_equal(out, _rotation(x, a.episodes)))
+    print(json.dumps({"workload": "exchange", "ctas": a.ctas, "elems": a.elems, "cluster": a.cluster,
+                      "global_stage": "lock-free flags" if a.lf else "atomic counter", "episodes": a.episodes,
+                      "ms": r.elapsed_ms, "episodes_per_s": r.episodes_per_s, "exchange_gbs": r.exchange_gbs,
+                      "bit_exact": exact}), flush=True)
+    return 0 if exact else 1
+
+
+def cmd_batch(a):
+    insts = batch_generate(seed=a.seed, n=a.n, iter_div=a.iter_div)
+    tb = Batch(batch_generate(seed=a.seed, n=a.n, iter_div=a.tune_div), mode="inc")
+    tb.autotune()
+    cl, se, v, _ = tb.get_plan()
+    tb.close()
+    b = Batch(insts, mode="inc")
+    rng = np.random.default_rng(a.seed)
+    inits = [rng.integers(0, 1000, size=b.words(i)).astype(np.uint32) for i in range(len(insts))]
+
+    def exact():
+        return all(np.array_equal(b.get_storage(i), expected_storage(
+            RunConfig(prim=p, num_ldst=L, num_tbs=G, num_iters=I, threads=256, repeats=1, mode="inc"), inits[i]))
+            for i, (p, L, G, I) in enumerate(insts))
+
+    for i, x in enumerate(inits):
+        b.set_storage(i, x)
+    rs = b.run_serial()
+    ok_serial = exact()
+    b.plan_ex(cl, se, v)
+    for i, x in enumerate(inits):
+        b.set_storage(i, x)
+    rb = b.run()
+    ok_batch = exact()
+    b.close()
+    print(json.dumps({"workload": "batch", "instances": len(insts), "ops": rb.ops,
+                      "per_launch_ms": rs.elapsed_ms, "batched_ms": rb.elapsed_ms,
+                      "ratio": rs.elapsed_ms / rb.elapsed_ms, "plan": [cl, se, v], "grid": rb.grid,
+                      "bit_exact": ok_serial and ok_batch}), flush=True)
+    return 0 if ok_serial and ok_batch else 1
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(prog="python -m heterosync_gb300.cli")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    e = sub.add_parser("exchange")
+    e.add_argument("--ctas", type=int, default=592)
+    e.add_argument("--elems", type=int, default=4096)
+    e.add_argument("--cluster", type=int, default=8)
+    e.add_argument("--lf", action="store_true")
+    e.add_argument("--episodes", type=int, default=1000)
+    e.add_argument("--seed", type=int, default=20260101)
+    bt = sub.add_parser("batch")
+    bt.add_argument("--seed", type=int, default=20260101)
+    bt.add_argument("--n", type=int, default=64)
+    bt.add_argument("--iter-div", type=int, default=1)
+    bt.add_argument("--tune-div", type=int, default=25)
+    a = ap.parse_args(argv)
+    return {"exchange": cmd_exchange, "batch": cmd_batch}[a.cmd](a)
+
+
+if __name__ == "__main__":
+    sys.exit(main())
