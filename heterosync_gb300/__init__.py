@@ -440,6 +440,140 @@ def exchange_run(buffers, cluster: int, lf: bool, episodes: int, timeout_ns: int
 
 
 # ---------------------------------------------------------------------------
+# Served request loop (hs_serve_*)
+# ---------------------------------------------------------------------------
+REQ_SYNCPRIM = 0
+
+
+class _ServeRequest(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("prim", ctypes.c_int), ("num_ldst", ctypes.c_int),
+                ("num_tbs", ctypes.c_int), ("num_iters", ctypes.c_int)]
+
+
+class _ServeCompletion(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_ulonglong), ("status", ctypes.c_int), ("dev_error_bits", ctypes.c_uint),
+                ("wait_site", ctypes.c_uint), ("latency_us", ctypes.c_double), ("service_us", ctypes.c_double),
+                ("admit_to_end_us", ctypes.c_double)]
+
+
+def _comp_dict(c):
+    return {"id": c.id, "status": c.status, "dev_error_bits": c.dev_error_bits, "wait_site": c.wait_site,
+            "latency_us": c.latency_us, "service_us": c.service_us, "admit_to_end_us": c.admit_to_end_us}
+
+
+class Server:
+    """A persistent server kernel admitting SyncPrims requests as they arrive.
+    While it runs, make no synchronising CUDA calls in this process."""
+
+    def __init__(self, slots: int = 32, gang: int = 8, arena_bytes: int = 1 << 30, staging_bytes: int = 1 << 30,
+                 idle_timeout_s: float = 60.0):
+        L = lib()
+        L.hs_serve_last_error.restype = ctypes.c_char_p
+        L.hs_serve_start.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong, ctypes.c_ulonglong,
+                                     ctypes.c_double, ctypes.c_void_p]
+        L.hs_serve_submit.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_void_p]
+        L.hs_serve_poll.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.hs_serve_pending.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.hs_serve_stop.argtypes = [ctypes.c_void_p, ctypes.c_double]
+        L.hs_serve_destroy.argtypes = [ctypes.c_void_p]
+        L.hs_serve_drive.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p,
+                                     ctypes.c_void_p]
+        L.hs_serve_request_words.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        h = ctypes.c_void_p()
+        s = L.hs_serve_start(slots, gang, arena_bytes, staging_bytes, idle_timeout_s, ctypes.byref(h))
+        if s:
+            raise HsError(s, L.hs_serve_last_error().decode())
+        self.h = h
+        self.slots, self.gang = slots, gang
+        self._keep = {}
+
+    def _check(self, s):
+        if s:
+            raise HsError(s, lib().hs_serve_last_error().decode())
+
+    @staticmethod
+    def request_words(prim, num_ldst, num_tbs, num_iters, nsm: int = 0):
+        nsm = nsm or device_info()["nsm"]
+        r = _ServeRequest(REQ_SYNCPRIM, prim_id(prim) if isinstance(prim, str) else prim, num_ldst, num_tbs,
+                          num_iters)
+        w = ctypes.c_size_t()
+        lib().hs_serve_request_words.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        s = lib().hs_serve_request_words(ctypes.byref(r), nsm, ctypes.byref(w))
+        if s:
+            raise HsError(s, "request words")
+        return int(w.value)
+
+    def submit(self, inst, init):
+        """inst = (prim, num_ldst, num_tbs, num_iters); init = the initial
+        storage (uint32).  Returns (id, output array filled at completion)."""
+        np = _np()
+        prim, L, G, I = inst
+        r = _ServeRequest(REQ_SYNCPRIM, prim_id(prim) if isinstance(prim, str) else prim, L, G, I)
+        init = np.ascontiguousarray(init, dtype=np.uint32)
+        out = np.zeros_like(init)
+        rid = ctypes.c_ulonglong()
+        self._check(lib().hs_serve_submit(self.h, ctypes.byref(r), _p(init), _p(out), ctypes.byref(rid)))
+        self._keep[rid.value] = out
+        return rid.value, out
+
+    def poll(self, max_n: int = 256):
+        buf = (_ServeCompletion * max_n)()
+        n = ctypes.c_int()
+        self._check(lib().hs_serve_poll(self.h, buf, max_n, ctypes.byref(n)))
+        res = []
+        for i in range(n.value):
+            d = _comp_dict(buf[i])
+            self._keep.pop(d["id"], None)
+            res.append(d)
+        return res
+
+    def wait(self, n: int, timeout_s: float = 120.0):
+        """Poll until n completions arrived (or the timeout)."""
+        import time
+        got, t0 = [], time.time()
+        while len(got) < n:
+            got += self.poll()
+            if time.time() - t0 > timeout_s:
+                raise HsError(2, "%d of %d completions after %.0f s" % (len(got), n, timeout_s))
+        return got
+
+    def drive(self, insts, inits, arrival_s, timeout_s: float = 300.0):
+        """Open-loop run: request i published at arrival_s[i]; returns
+        (outputs, completions in request order, wall seconds)."""
+        np = _np()
+        n = len(insts)
+        reqs = (_ServeRequest * n)(*[_ServeRequest(REQ_SYNCPRIM, p if not isinstance(p, str) else prim_id(p), L, G, I)
+                                     for (p, L, G, I) in insts])
+        ins = [np.ascontiguousarray(x, dtype=np.uint32) for x in inits]
+        outs = [np.zeros_like(x) for x in ins]
+        in_p = (ctypes.c_void_p * n)(*[x.ctypes.data for x in ins])
+        out_p = (ctypes.c_void_p * n)(*[x.ctypes.data for x in outs])
+        arr = np.ascontiguousarray(arrival_s, dtype=np.float64)
+        comps = (_ServeCompletion * n)()
+        wall = ctypes.c_double()
+        self._check(lib().hs_serve_drive(self.h, reqs, n, in_p, out_p, _p(arr), timeout_s, comps,
+                                         ctypes.byref(wall)))
+        return outs, [_comp_dict(c) for c in comps], wall.value
+
+    def stop(self, timeout_s: float = 120.0):
+        if self.h:
+            self._check(lib().hs_serve_stop(self.h, timeout_s))
+
+    def close(self):
+        if self.h:
+            lib().hs_serve_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+
+# ---------------------------------------------------------------------------
 # Batched mixed instances (hs_batch_*)
 # ---------------------------------------------------------------------------
 class _BatchInst(ctypes.Structure):

@@ -39,6 +39,7 @@ CU_SOURCES = [
     "hs_uts.cu",
     "hs_batch.cu",
     "hs_exchange.cu",
+    "hs_serve.cu",
 ]
 # command-line programs: (output name, source)
 PROGRAMS = [

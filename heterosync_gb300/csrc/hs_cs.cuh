@@ -130,6 +130,7 @@ struct TmaCtx {
   unsigned char* buf;  // dynamic shared memory, chunk bytes
   unsigned mbar;       // shared address of the mbarrier
   unsigned phase;
+  unsigned cap;        // bytes of buf (tiled paths)
 };
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -138,6 +139,7 @@ __device__ __forceinline__ void tma_init(TmaCtx& t, unsigned long long* mbar_sto
   t.buf = dyn;
   t.mbar = smem_addr(mbar_storage);
   t.phase = 0;
+  t.cap = 0;
   if (is_master()) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(t.mbar) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");

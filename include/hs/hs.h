@@ -248,6 +248,49 @@ int hs_exchange_fill(unsigned long long seed, size_t words, uint32_t* out);
 int hs_exchange_run(const uint32_t* host_in, uint32_t* host_out, int n, int elems, int cluster, int lf, int episodes,
                     unsigned long long timeout_ns, hs_exchange_result* r);
 
+/* ---- served request loop -------------------------------------------------------- */
+/* A persistent server kernel of `slots` slots x `gang` co-resident CTAs admits
+ * requests as they arrive (oldest first, when a slot is free and the device
+ * arena has pages for the request's storage and lock state), executes each on
+ * its slot's CTAs and publishes a completion.  No counterpart in the reference
+ * (whose programs run one instance per launch); the instances themselves are
+ * its SyncPrims (main.cu:104-836) in increment mode, 256 threads per TB.
+ * Between hs_serve_start and hs_serve_stop the server kernel occupies the
+ * device: the process must not make synchronising CUDA calls on it
+ * (cudaDeviceSynchronize, cudaMalloc, cudaFree) until the server stopped. */
+enum { HS_REQ_SYNCPRIM = 0 };
+typedef struct hs_serve_request {
+  int kind;                                  /* HS_REQ_SYNCPRIM */
+  int prim, num_ldst, num_tbs, num_iters;    /* the instance */
+} hs_serve_request;
+typedef struct hs_serve_completion {
+  unsigned long long id;
+  int status;                 /* HS_OK; HS_ENORES: larger than the arena; HS_ETIMEDOUT: a wait ran out */
+  unsigned dev_error_bits, wait_site;
+  double latency_us;          /* submission (or due time, hs_serve_drive) to completion seen by the host */
+  double service_us;          /* on the device: state laid out -> final storage copied back */
+  double admit_to_end_us;     /* on the device: admission -> completion */
+} hs_serve_completion;
+typedef struct hs_server hs_server;
+const char* hs_serve_last_error(void);
+int hs_serve_start(int slots, int gang, unsigned long long arena_bytes, unsigned long long staging_bytes,
+                   double idle_timeout_s, hs_server** out);
+int hs_serve_request_words(const hs_serve_request* r, int nsm, size_t* words);
+/* Copies `input` (the instance's initial storage) into the staging pool and
+ * publishes the request; `output` receives the final storage when
+ * hs_serve_poll returns its completion.  HS_ENORES: ring or staging pool full. */
+int hs_serve_submit(hs_server* s, const hs_serve_request* r, const uint32_t* input, uint32_t* output,
+                    unsigned long long* id);
+int hs_serve_poll(hs_server* s, hs_serve_completion* out, int max, int* n);
+int hs_serve_pending(hs_server* s, unsigned long long* in_flight);
+int hs_serve_stop(hs_server* s, double timeout_s);
+int hs_serve_destroy(hs_server* s);
+/* Open-loop driver: request i is published at arrival_s[i] seconds after the
+ * start; comps[i] receives its completion (latency from the due time). */
+int hs_serve_drive(hs_server* s, const hs_serve_request* reqs, int n, const uint32_t* const* inputs,
+                   uint32_t* const* outputs, const double* arrival_s, double timeout_s, hs_serve_completion* comps,
+                   double* wall_s);
+
 /* ---- roofline probes --------------------------------------------------------- */
 /* Aggregate L2 atomic rate: blocks x threads threads each issue `iters`
  * red.add to their own 128-byte-spaced word (same_address = 0: contention-free

@@ -1,0 +1,128 @@
+"""GPU: the served request loop.  SyncPrims requests admitted into the
+persistent server kernel's slots as they arrive; every result is compared with
+the closed form of the reference golden, alone (one request at a time) and in
+a mix (many in flight, overlapping on the device), and the two must agree."""
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+PRIMS = [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30, 31]
+
+
+def _expected(hs, inst, init):
+    p, L, G, I = inst
+    cfg = hs.RunConfig(prim=p, num_ldst=L, num_tbs=G, num_iters=I, threads=256, repeats=1, mode="inc")
+    return hs.expected_storage(cfg, init)
+
+
+def _requests(hs, seed):
+    insts = [(p, 3 + (p * 7) % 40, 2 + (p * 5) % 37, 2 + p % 5) for p in PRIMS]
+    insts += hs.batch_generate(seed=seed, n=16, iter_div=400)
+    rng = np.random.default_rng(seed)
+    nsm = hs.device_info()["nsm"]
+    inits = [rng.integers(0, 2 ** 32, size=hs.Server.request_words(*x, nsm=nsm), dtype=np.uint64).astype(np.uint32)
+             for x in insts]
+    return insts, inits
+
+
+def _submit_all(srv, insts, inits):
+    outs = {}
+    for x, a in zip(insts, inits):
+        while True:
+            try:
+                rid, out = srv.submit(x, a)
+                outs[rid] = out
+                break
+            except Exception as e:  # ring or staging pool full: let completions drain
+                if getattr(e, "status", None) != 3:
+                    raise
+                time.sleep(0.001)
+    return outs
+
+
+def test_alone_and_in_mix_agree(hs):
+    insts, inits = _requests(hs, 101)
+    srv = hs.Server(slots=8, gang=4, arena_bytes=256 << 20, staging_bytes=256 << 20, idle_timeout_s=20.0)
+    try:
+        alone = []
+        for x, a in zip(insts, inits):
+            rid, out = srv.submit(x, a)
+            c = srv.wait(1)[0]
+            assert c["id"] == rid and c["status"] == 0, (x, c)
+            alone.append(out.copy())
+        ids = list(_submit_all(srv, insts, inits).items())
+        comps = {c["id"]: c for c in srv.wait(len(insts))}
+        for k, (rid, out) in enumerate(ids):
+            assert comps[rid]["status"] == 0, (insts[k], comps[rid])
+            want = _expected(hs, insts[k], inits[k])
+            assert np.array_equal(alone[k], want), ("alone", insts[k])
+            assert np.array_equal(out, want), ("mix", insts[k])
+        srv.stop()
+    finally:
+        srv.close()
+
+
+def test_admission_waits_for_device_memory(hs):
+    """An arena that holds only a few requests at a time: admission waits for
+    pages, every request still completes exactly; one larger than the whole
+    arena is rejected with HS_ENORES."""
+    insts = [(4, 64, 96, 3), (10, 48, 200, 2), (1, 32, 152, 2), (22, 64, 64, 3)] * 4
+    rng = np.random.default_rng(7)
+    nsm = hs.device_info()["nsm"]
+    inits = [rng.integers(0, 1000, size=hs.Server.request_words(*x, nsm=nsm)).astype(np.uint32) for x in insts]
+    biggest = max(a.size for a in inits) * 4
+    srv = hs.Server(slots=8, gang=2, arena_bytes=3 * biggest + (1 << 20), staging_bytes=256 << 20,
+                    idle_timeout_s=20.0)
+    try:
+        ids = list(_submit_all(srv, insts, inits).items())
+        big = (1, 128, 512, 1)  # a barrier instance: 512 chunks, about 67 MB
+        big_init = np.zeros(hs.Server.request_words(*big, nsm=nsm), np.uint32)
+        big_id, _ = srv.submit(big, big_init)
+        comps = {c["id"]: c for c in srv.wait(len(insts) + 1)}
+        assert comps[big_id]["status"] == 3
+        for k, (rid, out) in enumerate(ids):
+            assert comps[rid]["status"] == 0
+            assert np.array_equal(out, _expected(hs, insts[k], inits[k])), insts[k]
+        srv.stop()
+    finally:
+        srv.close()
+
+
+def test_open_loop_drive(hs):
+    insts, inits = _requests(hs, 202)
+    rng = np.random.default_rng(3)
+    arrivals = np.cumsum(rng.exponential(0.0005, size=len(insts)))
+    srv = hs.Server(slots=16, gang=4, arena_bytes=512 << 20, staging_bytes=256 << 20, idle_timeout_s=20.0)
+    try:
+        outs, comps, wall = srv.drive(insts, inits, arrivals)
+        srv.stop()
+    finally:
+        srv.close()
+    assert wall > 0
+    for k, x in enumerate(insts):
+        assert comps[k]["status"] == 0 and comps[k]["latency_us"] > 0
+        assert np.array_equal(outs[k], _expected(hs, x, inits[k])), x
+
+
+def test_stop_drains_then_idle_exit(hs):
+    insts, inits = _requests(hs, 303)
+    srv = hs.Server(slots=4, gang=4, arena_bytes=256 << 20, staging_bytes=128 << 20, idle_timeout_s=20.0)
+    try:
+        ids = list(_submit_all(srv, insts[:12], inits[:12]).items())
+        srv.stop()  # returns once every published request was admitted and the kernel exited
+        comps = {c["id"]: c for c in srv.wait(len(ids), timeout_s=5.0)}
+        for k, (rid, out) in enumerate(ids):
+            assert comps[rid]["status"] == 0
+            assert np.array_equal(out, _expected(hs, insts[k], inits[k]))
+    finally:
+        srv.close()
+    # a server with no requests ends by itself after its idle limit
+    srv = hs.Server(slots=2, gang=2, arena_bytes=16 << 20, staging_bytes=16 << 20, idle_timeout_s=0.2)
+    try:
+        time.sleep(0.6)
+        srv.stop(timeout_s=5.0)
+    finally:
+        srv.close()
