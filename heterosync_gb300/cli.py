@@ -5,6 +5,12 @@
       tree barrier with local exchange on thread-block clusters; prints one
       JSON line (episodes/s, exchange GB/s, bit-exact check of the rotation)
 
+  python -m heterosync_gb300.cli serve [--n 256] [--iter-div 50] [--slots 64]
+         [--gang 8] [--loads 10,30,50,70,90]
+      the served request loop: peak request rate, then Poisson arrivals at
+      each offered load; p50/p99 latency, throughput, the offline batch of the
+      same requests, bit-exact check of every result
+
   python -m heterosync_gb300.cli batch [--seed 20260101] [--n 64]
          [--iter-div 1] [--tune-div 25]
       the mixed-instance batch: one launch per instance, then the autotuned
@@ -69,6 +75,15 @@ def cmd_batch(a):
     return 0 if ok_serial and ok_batch else 1
 
 
+def cmd_serve(a):
+    from .served import served_sweep
+    loads = tuple(float(x) / 100.0 for x in a.loads.split(","))
+    r = served_sweep(seed=a.seed, n=a.n, iter_div=a.iter_div, slots=a.slots, gang=a.gang, loads=loads,
+                     offline=not a.no_offline)
+    print(json.dumps({"workload": "serve", **r}), flush=True)
+    return 0 if r["bit_exact"] else 1
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m heterosync_gb300.cli")
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -84,8 +99,16 @@ def main(argv=None):
     bt.add_argument("--n", type=int, default=64)
     bt.add_argument("--iter-div", type=int, default=1)
     bt.add_argument("--tune-div", type=int, default=25)
+    sv = sub.add_parser("serve")
+    sv.add_argument("--seed", type=int, default=20260101)
+    sv.add_argument("--n", type=int, default=256)
+    sv.add_argument("--iter-div", type=int, default=50)
+    sv.add_argument("--slots", type=int, default=64)
+    sv.add_argument("--gang", type=int, default=8)
+    sv.add_argument("--loads", default="10,30,50,70,90", help="offered loads, percent of the measured peak")
+    sv.add_argument("--no-offline", action="store_true")
     a = ap.parse_args(argv)
-    return {"exchange": cmd_exchange, "batch": cmd_batch}[a.cmd](a)
+    return {"exchange": cmd_exchange, "batch": cmd_batch, "serve": cmd_serve}[a.cmd](a)
 
 
 if __name__ == "__main__":

@@ -154,6 +154,23 @@ __device__ __forceinline__ bool mbar_done(unsigned mbar, unsigned phase) {
   return done != 0;
 }
 
+// Wait for this CTA's own bulk copy.  The copy completes in hardware whatever
+// other CTAs do, so this wait does not give up when another CTA has already
+// failed (abandoning it would leave the copy writing into shared memory and the
+// mbarrier a phase ahead of its owner); it has only its own time limit.
+constexpr unsigned long long kTmaWaitNs = 1000000000ull;
+__device__ __forceinline__ bool tma_wait(const TmaCtx& t, const HsEnv& env) {
+  if (mbar_done(t.mbar, t.phase)) return true;
+  const unsigned long long t0 = globaltimer();
+  for (unsigned i = 1;; ++i) {
+    if (mbar_done(t.mbar, t.phase)) return true;
+    if ((i & 63u) == 0u && globaltimer() - t0 > kTmaWaitNs) {
+      fail(env, HS_DEV_TIMEOUT, HS_SITE_TMA);
+      return false;
+    }
+  }
+}
+
 // Load a chunk into shared memory; returns the CTA-wide success.
 __device__ __forceinline__ bool tma_load_chunk(const unsigned* chunk, unsigned bytes, TmaCtx& t, const HsEnv& env) {
   if (is_master()) {
@@ -162,7 +179,7 @@ __device__ __forceinline__ bool tma_load_chunk(const unsigned* chunk, unsigned b
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                  :: "r"(smem_addr(t.buf)), "l"(chunk), "r"(bytes), "r"(t.mbar) : "memory");
   }
-  const bool ok = wait_until([&] { return mbar_done(t.mbar, t.phase); }, [] {}, env, HS_SITE_TMA);
+  const bool ok = is_master() ? tma_wait(t, env) : true;
   t.phase ^= 1u;
   return __syncthreads_and(ok) != 0;
 }

@@ -133,6 +133,7 @@ __device__ __noinline__ bool cl_sem_op(const RunDesc& d, int b, int cr, int cl, 
 
 // Counter barrier among the gang's CTAs (instance's global barrier lines).
 __device__ __forceinline__ bool gang_barrier(const RunDesc& d, unsigned n, unsigned& gen, const HsEnv& env) {
+  __syncthreads();  // every thread's critical-section stores precede the master's release
   int ok = 1;
   if (is_master()) {
     bool okb = true;

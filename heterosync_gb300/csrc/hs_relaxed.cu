@@ -222,6 +222,7 @@ __global__ void __launch_bounds__(256) k_flags(unsigned* stop, unsigned* dirty, 
     }
   }
   // grid barrier: every TB must have stopped before the main TB reads dirty
+  __syncthreads();
   int ok = 1;
   if (is_master()) {
     bool okb = true;

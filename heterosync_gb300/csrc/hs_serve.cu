@@ -75,8 +75,9 @@ struct ServeComp {
 };
 
 struct ServeHostCtl {  // mapped host memory; the host writes
-  unsigned long long tail;  // requests published
-  unsigned long long stop;  // nonzero: exit once the ring is drained
+  unsigned long long tail;   // requests published
+  unsigned long long stop;   // nonzero: exit once the ring is drained
+  unsigned long long abort;  // nonzero: exit now (server waits give up)
 };
 
 struct ServeRec {  // one live page allocation
@@ -170,14 +171,37 @@ __device__ void arena_free(const ServeArgs& a, unsigned long long rec) {
   else c->a_tail = a.recs[c->rec_tail % a.n_recs].start;
 }
 
-// Counter barrier among the slot's CTAs (generation-valued, no resets).
-__device__ __forceinline__ bool slot_barrier(SlotBox* box, int gang, unsigned& gen, const HsEnv& env) {
+// Counter barrier among the slot's CTAs (generation-valued, no resets).  Its
+// wait also gives up when the host raises the abort word.
+__device__ __forceinline__ bool slot_barrier(SlotBox* box, int gang, unsigned& gen, const HsEnv& env,
+                                             const ServeHostCtl* hctl) {
+  __syncthreads();  // every thread's stores (state, storage) precede the master's release
   int ok = 1;
   if (is_master()) {
-    bool okb = true;
-    counter_barrier<GPU>(box->bar, box->bar + kLineWords, (unsigned)gang, gen, 256u, env, HS_SITE_SERVE,
-                         [] { return true; }, &okb);
-    ok = okb;
+    unsigned* count = box->bar;
+    unsigned* genw = box->bar + kLineWords;
+    const unsigned old = atom_add_acqrel<GPU>(count, 1u);
+    if (old == (unsigned)gang - 1u) {
+      st_relaxed<GPU>(count, 0u);
+      st_release<GPU>(genw, gen + 1u);
+    } else {
+      const unsigned long long t0 = globaltimer();
+      for (unsigned i = 1;; ++i) {
+        if (ld_acquire<GPU>(genw) != gen) break;
+        sleep_ns(256);
+        if ((i & 63u) == 0u) {
+          if (ld_relaxed<GPU>(env.status) != 0u || ld_relaxed_sys64(&hctl->abort) != 0ull) {
+            ok = 0;
+            break;
+          }
+          if (globaltimer() - t0 > env.timeout_ns) {
+            fail(env, HS_DEV_TIMEOUT, HS_SITE_SERVE);
+            ok = 0;
+            break;
+          }
+        }
+      }
+    }
   }
   gen += 1u;
   return __syncthreads_or(!ok) == 0;
@@ -195,7 +219,7 @@ __device__ int serve_admit(const ServeArgs& a, SlotBox* box, const HsEnv& env) {
       const unsigned long long tail = ld_acquire_sys64(&a.hctl->tail);
       const unsigned long long head = *reinterpret_cast<volatile unsigned long long*>(&a.ctl->qhead);
       s_cmd = head < tail ? CMD_RUN : (ld_relaxed_sys64(&a.hctl->stop) ? CMD_STOP : CMD_IDLE);
-      if (ld_relaxed<GPU>(env.status) != 0u) s_cmd = CMD_STOP;
+      if (ld_relaxed<GPU>(env.status) != 0u || ld_relaxed_sys64(&a.hctl->abort) != 0ull) s_cmd = CMD_STOP;
     }
     __syncthreads();
     int cmd = s_cmd;
@@ -339,7 +363,7 @@ __global__ void __launch_bounds__(kServeThreads, 4) k_serve(ServeArgs a) {
       }
       if (is_master()) box->cmd = cmd;
     }
-    if (!slot_barrier(box, a.gang, gen, senv)) break;
+    if (!slot_barrier(box, a.gang, gen, senv, a.hctl)) break;
     // the box was rewritten for this request: read it at gpu scope (no stale
     // L1 line from an earlier request) and share it through shared memory
     constexpr int kBW = (int)(offsetof(SlotBox, bar) / 8);
@@ -365,7 +389,7 @@ __global__ void __launch_bounds__(kServeThreads, 4) k_serve(ServeArgs a) {
       const size_t sw = sb.state_words;
       const unsigned groups = sb.groups, rgroups = sb.ring_groups;
       for (size_t w = gtid; w < sw; w += gstride) base[w] = state_init_value(d, base, w, groups, rgroups);
-      if (!slot_barrier(box, a.gang, gen, senv)) break;
+      if (!slot_barrier(box, a.gang, gen, senv, a.hctl)) break;
       t_start = globaltimer();
       const HsEnv env{d.status, d.timeout_ns};
       if (is_mutex_prim(d.prim) || is_sem_prim(d.prim)) {
@@ -378,11 +402,11 @@ __global__ void __launch_bounds__(kServeThreads, 4) k_serve(ServeArgs a) {
       } else {
         batch_barrier<MODE>(d, rank, a.gang, 0u, tma, env);
       }
-      if (!slot_barrier(box, a.gang, gen, senv)) break;
+      if (!slot_barrier(box, a.gang, gen, senv, a.hctl)) break;
       copy_words(reinterpret_cast<unsigned*>(a.staging + stage_off), d.data, words, gtid, gstride);
       __syncthreads();
       if (is_master()) __threadfence_system();
-      if (!slot_barrier(box, a.gang, gen, senv)) break;
+      if (!slot_barrier(box, a.gang, gen, senv, a.hctl)) break;
     }
     if (rank == 0) {
       if (is_master()) {
@@ -734,12 +758,21 @@ extern "C" int hs_serve_stop(hs_server* S, double timeout_s) {
   if (!S) return HS_EINVAL;
   if (!S->running) return HS_OK;
   __atomic_store_n(&S->hctl->stop, 1ull, __ATOMIC_RELEASE);
-  const double t0 = now_s();
+  double t0 = now_s();
   cudaError_t e = cudaErrorNotReady;
+  bool aborted = false;
   while ((e = cudaStreamQuery(S->stream)) == cudaErrorNotReady) {
     if (now_s() - t0 > timeout_s) {
-      g_serr = "server did not stop in time";
-      return HS_ETIMEDOUT;
+      if (aborted) {
+        g_serr = "server did not stop in time";
+        return HS_ETIMEDOUT;  // still running: its memory stays allocated
+      }
+      // not drained in time: make every server wait give up (a running
+      // instance still ends within its own wait limit)
+      __atomic_store_n(&S->hctl->abort, 1ull, __ATOMIC_RELEASE);
+      aborted = true;
+      t0 = now_s();
+      timeout_s = 60.0;
     }
     std::this_thread::sleep_for(std::chrono::microseconds(200));
   }
@@ -750,8 +783,8 @@ extern "C" int hs_serve_stop(hs_server* S, double timeout_s) {
   }
   unsigned st[2] = {0, 0};
   cudaMemcpy(st, reinterpret_cast<ServeCtl*>(S->dev)->status, sizeof(st), cudaMemcpyDeviceToHost);
-  if (st[0]) {
-    g_serr = "server wait timed out";
+  if (st[0] || aborted) {
+    g_serr = aborted ? "server aborted before its ring drained" : "server wait timed out";
     return HS_ETIMEDOUT;
   }
   return HS_OK;

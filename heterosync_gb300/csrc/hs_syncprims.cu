@@ -130,6 +130,7 @@ __device__ __forceinline__ bool local_only_barrier(const RunDesc& d, int g, int 
   unsigned* lgen = group_line(d, g, 1);
   unsigned* lgo = group_line(d, g, 2);
   unsigned* lflags = d.locks + (size_t)(d.l_lflag + g * d.lflag_lines) * kLineWords;
+  __syncthreads();  // every thread's critical-section stores precede the master's release
   int ok = 1;
   if constexpr (!LF) {
     if (is_master()) {
@@ -165,6 +166,7 @@ __device__ __forceinline__ bool tree_barrier(const RunDesc& d, int g, int r, int
   unsigned* ggenw = d.locks + (size_t)(d.l_glob + 1) * kLineWords;
   unsigned* ggo = d.locks + (size_t)(d.l_glob + 2) * kLineWords;
   unsigned* gflags = d.locks + (size_t)d.l_gflag * kLineWords;
+  __syncthreads();  // every thread's critical-section stores precede the master's release
   int ok = 1;
   if constexpr (!LF) {
     if (m == 1) {  // no local stage
