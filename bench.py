@@ -21,7 +21,9 @@ Beside the sweep, outside its timed region, the line carries "exchange" (tree
 barrier with local exchange on thread-block clusters: 592 CTAs, fp32[4096] per
 CTA rotated every episode, 1000 episodes, cluster sizes 1/2/4/8) and "batch"
 (the 64-instance mixed batch, one launch per instance against the autotuned
-persistent graph-replayed launch); --no-extras skips both.
+persistent graph-replayed launch) and "serve" (the served request loop: peak
+request rate, p50/p99 latency under Poisson arrivals at 10-90% of it); the
+extras run outside the sweep's timed region; --no-extras skips them.
 
 --impl reference runs the reference's own SyncPrims kernels (built from its
 unmodified sources into oracle/_ref) on the same GPU with the same sizes, each
@@ -291,6 +293,18 @@ def batch_extra(hs):
                      "tuned_on": "numCSIters / 25 (%.1f ms)" % tune_ms}}
 
 
+def serve_extra(hs):
+    """Served request loop: 256 requests from the mixed-instance generator
+    (numCSIters / 50), 64 slots of 8-CTA clusters; peak request rate, then
+    Poisson arrivals at 10-90% of it; p50/p99 latency from each request's due
+    time; the offline batch of the same requests; every result bit-exact."""
+    from heterosync_gb300.served import served_sweep
+    r = served_sweep(seed=SEED, n=256, iter_div=50, slots=64, gang=8)
+    if not r["bit_exact"]:
+        raise SystemExit("bench: a served request's result differs from the expected final storage")
+    return r
+
+
 def reference_arm(args, rank):
     import oracle
     hs_nsm = None
@@ -484,7 +498,7 @@ def main():
         if ck:
             out["clocks"] = ck
         if not args.no_extras and world == 1:
-            for key, fn in (("exchange", exchange_extra), ("batch", batch_extra)):
+            for key, fn in (("exchange", exchange_extra), ("batch", batch_extra), ("serve", serve_extra)):
                 try:
                     out[key] = fn(hs)
                 except SystemExit:

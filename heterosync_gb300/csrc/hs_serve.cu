@@ -314,7 +314,13 @@ __device__ __forceinline__ unsigned state_init_value(const RunDesc& d, const uns
   return 0u;
 }
 
-template <int MODE>
+// CL: the slot is a thread-block cluster of `gang` CTAs.  Its slot barriers are
+// then the hardware cluster barrier (every CTA's work between two of them is
+// bounded, and every CTA leaves the loop at the same barrier, on the command
+// its rank 0 published), and a serialised instance (global mutex or
+// semaphore) with numLdSt >= 33 runs as one cluster-wide executor that splits
+// each critical section over the slot's SMs.
+template <int MODE, bool CL>
 __global__ void __launch_bounds__(kServeThreads, 4) k_serve(ServeArgs a) {
   __shared__ int s_slot;
   __shared__ int s_ok[9];
@@ -327,6 +333,14 @@ __global__ void __launch_bounds__(kServeThreads, 4) k_serve(ServeArgs a) {
   SlotBox* box = a.boxes + slot;
   const HsEnv senv{a.ctl->status, a.slot_ns};
   unsigned gen = 0;
+  auto sbar = [&]() -> bool {
+    if constexpr (CL) {
+      cluster_sync_all();
+      return true;
+    } else {
+      return slot_barrier(box, a.gang, gen, senv, a.hctl);
+    }
+  };
   const unsigned tid = threadIdx.x, nthr = blockDim.x;
   const size_t gtid = (size_t)rank * nthr + tid, gstride = (size_t)a.gang * nthr;
   for (;;) {
@@ -363,7 +377,7 @@ __global__ void __launch_bounds__(kServeThreads, 4) k_serve(ServeArgs a) {
       }
       if (is_master()) box->cmd = cmd;
     }
-    if (!slot_barrier(box, a.gang, gen, senv, a.hctl)) break;
+    if (!sbar()) break;
     // the box was rewritten for this request: read it at gpu scope (no stale
     // L1 line from an earlier request) and share it through shared memory
     constexpr int kBW = (int)(offsetof(SlotBox, bar) / 8);
@@ -389,24 +403,27 @@ __global__ void __launch_bounds__(kServeThreads, 4) k_serve(ServeArgs a) {
       const size_t sw = sb.state_words;
       const unsigned groups = sb.groups, rgroups = sb.ring_groups;
       for (size_t w = gtid; w < sw; w += gstride) base[w] = state_init_value(d, base, w, groups, rgroups);
-      if (!slot_barrier(box, a.gang, gen, senv, a.hctl)) break;
+      if (!sbar()) break;
       t_start = globaltimer();
       const HsEnv env{d.status, d.timeout_ns};
       if (is_mutex_prim(d.prim) || is_sem_prim(d.prim)) {
         const bool mtx = is_mutex_prim(d.prim);
+        const bool whole = CL && d.prim >= 4 && d.prim <= 15 && d.L >= 33;
+        const int ecl = whole ? a.gang : 1, er = whole ? rank : 0;
+        const int execs = a.gang / ecl, x = rank / ecl;
         bool ok = true;
         for (int j = 0; j < d.iters && ok; ++j)
-          for (int b = rank; b < d.num_tbs && ok; b += a.gang)
-            ok = mtx ? cl_mutex_op<MODE>(d, b, 0, 1, &s_slot, s_ok, tma, env)
-                     : cl_sem_op<MODE>(d, b, 0, 1, s_ok, tma, env);
+          for (int b = x; b < d.num_tbs && ok; b += execs)
+            ok = mtx ? cl_mutex_op<MODE>(d, b, er, ecl, &s_slot, s_ok, tma, env)
+                     : cl_sem_op<MODE>(d, b, er, ecl, s_ok, tma, env);
       } else {
         batch_barrier<MODE>(d, rank, a.gang, 0u, tma, env);
       }
-      if (!slot_barrier(box, a.gang, gen, senv, a.hctl)) break;
+      if (!sbar()) break;
       copy_words(reinterpret_cast<unsigned*>(a.staging + stage_off), d.data, words, gtid, gstride);
       __syncthreads();
       if (is_master()) __threadfence_system();
-      if (!slot_barrier(box, a.gang, gen, senv, a.hctl)) break;
+      if (!sbar()) break;
     }
     if (rank == 0) {
       if (is_master()) {
@@ -427,9 +444,12 @@ __global__ void __launch_bounds__(kServeThreads, 4) k_serve(ServeArgs a) {
         st_release_sys64(&r->seq, k + 1ull);
       }
       if (cmd == CMD_RUN) {
-        if (!ticket_lock<GPU>(a.ctl->lock, a.ctl->lock + kLineWords, kTicketWrap, 0u, 0u, senv)) break;
-        if (is_master()) arena_free(a, rec);
-        ticket_unlock<GPU>(a.ctl->lock + kLineWords, kTicketWrap);
+        if (ticket_lock<GPU>(a.ctl->lock, a.ctl->lock + kLineWords, kTicketWrap, 0u, 0u, senv)) {
+          if (is_master()) arena_free(a, rec);
+          ticket_unlock<GPU>(a.ctl->lock + kLineWords, kTicketWrap);
+        } else if (!CL) {
+          break;  // the server status is set: the next admission stops every slot
+        }
       }
     }
   }
@@ -530,18 +550,42 @@ extern "C" int hs_serve_start(int slots, int gang, unsigned long long arena_byte
   S->slots = slots;
   S->gang = gang;
   cudaDeviceGetAttribute(&S->nsm, cudaDevAttrMultiProcessorCount, dev);
-  auto fn = k_serve<M_INC>;
-  if (cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kServeStage) !=
-      cudaSuccess) {
+  // slots of 2, 4 or 8 CTAs run as thread-block clusters
+  const bool cl = gang == 2 || gang == 4 || gang == 8;
+  const void* fn = cl ? (const void*)k_serve<M_INC, true> : (const void*)k_serve<M_INC, false>;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kServeStage) != cudaSuccess) {
     g_serr = "shared memory attribute";
     delete S;
     return HS_ECUDA;
   }
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kServeThreads, kServeStage);
-  if ((long long)slots * gang > (long long)per_sm * S->nsm) {
-    g_serr = std::to_string(slots * gang) + " server CTAs cannot all be resident (" + std::to_string(per_sm * S->nsm) +
-             ")";
+  cudaLaunchConfig_t lc = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cl ? (unsigned)gang : 1u;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  lc.gridDim = dim3((unsigned)(slots * gang));
+  lc.blockDim = dim3((unsigned)kServeThreads);
+  lc.dynamicSmemBytes = kServeStage;
+  lc.attrs = attr;
+  lc.numAttrs = cl ? 1 : 0;
+  long long capacity = 0;
+  if (cl) {
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, fn, &lc) != cudaSuccess) {
+      cudaGetLastError();
+      g_serr = "cluster occupancy query failed";
+      delete S;
+      return HS_ECUDA;
+    }
+    capacity = (long long)clusters * gang;
+  } else {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kServeThreads, kServeStage);
+    capacity = (long long)per_sm * S->nsm;
+  }
+  if ((long long)slots * gang > capacity) {
+    g_serr = std::to_string(slots * gang) + " server CTAs cannot all be resident (" + std::to_string(capacity) + ")";
     delete S;
     return HS_ENORES;
   }
@@ -588,8 +632,8 @@ extern "C" int hs_serve_start(int slots, int gang, unsigned long long arena_byte
   a.idle_ns = (unsigned long long)(idle_timeout_s * 1e9);
   a.slot_ns = a.idle_ns + 120000000000ull;  // a slot waits for its own CTAs (admission, then one instance)
   void* args[] = {&a};
-  if (cudaLaunchKernel((const void*)fn, dim3((unsigned)(slots * gang)), dim3(kServeThreads), args, kServeStage,
-                       S->stream) != cudaSuccess) {
+  lc.stream = S->stream;
+  if (cudaLaunchKernelExC(&lc, fn, args) != cudaSuccess) {
     g_serr = "server launch failed";
     serve_free(S);
     return HS_ECUDA;
