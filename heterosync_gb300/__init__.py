@@ -399,6 +399,39 @@ def uts_run(tree, frontier, host_processed: int, blocks: int, threads: int = 128
 
 
 # ---------------------------------------------------------------------------
+# Geometric UTS with a SHA-1 node generator (hs_uts_geo_*)
+# ---------------------------------------------------------------------------
+class _GeoResult(ctypes.Structure):
+    _fields_ = [("nodes", ctypes.c_ulonglong), ("leaves", ctypes.c_ulonglong), ("max_depth", ctypes.c_uint),
+                ("elapsed_ms", ctypes.c_float), ("dev_error_bits", ctypes.c_uint)]
+
+
+def uts_geo_table(branching: float = 4.0, n: int = 128):
+    np = _np()
+    t = np.zeros(n, dtype=np.uint32)
+    lib().hs_uts_geo_table.argtypes = [ctypes.c_double, ctypes.c_void_p, ctypes.c_int]
+    nz = lib().hs_uts_geo_table(branching, _p(t), n)
+    if nz < 0:
+        raise HsError(1, "geo table")
+    return t, nz
+
+
+def uts_geo_run(seed: int, depth_limit: int, branching: float = 4.0, blocks: int = 0, threads: int = 256,
+                timeout_ns: int = 0):
+    """Count the geometric tree on the GPU: (nodes, leaves, deepest level, ms)."""
+    blocks = blocks or device_info()["nsm"] * 4
+    r = _GeoResult()
+    L = lib()
+    L.hs_uts_geo_last_error.restype = ctypes.c_char_p
+    L.hs_uts_geo_run.argtypes = [ctypes.c_uint, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                 ctypes.c_ulonglong, ctypes.c_void_p]
+    s = L.hs_uts_geo_run(seed, depth_limit, branching, blocks, threads, timeout_ns, ctypes.byref(r))
+    if s:
+        raise HsError(s, L.hs_uts_geo_last_error().decode())
+    return r.nodes, r.leaves, r.max_depth, r.elapsed_ms
+
+
+# ---------------------------------------------------------------------------
 # Tree barrier with local exchange on thread-block clusters (hs_exchange_*)
 # ---------------------------------------------------------------------------
 class _ExchResult(ctypes.Structure):

@@ -40,6 +40,7 @@ CU_SOURCES = [
     "hs_batch.cu",
     "hs_exchange.cu",
     "hs_serve.cu",
+    "hs_uts_geo.cu",
 ]
 # command-line programs: (output name, source)
 PROGRAMS = [

@@ -225,6 +225,27 @@ int hs_uts_frontier(const hs_uts_node* tree, int num_nodes, int cores_used, int*
 int hs_uts_run(const hs_uts_node* tree, int num_nodes, const int* frontier, int n_frontier, unsigned host_processed,
                int blocks, int threads, unsigned long long timeout_ns, hs_uts_result* out);
 
+/* ---- geometric UTS with a SHA-1 node generator ----------------------------------- */
+/* No counterpart in the reference repository (its UTS is the rand() binary
+ * tree, hs_uts_run): the published Unbalanced Tree Search geometric tree.
+ * root = SHA-1(16 zero bytes || seed), child i = SHA-1(parent || i) (4-byte
+ * big-endian integers), r = last state word & 0x7fffffff, children = 0 at
+ * depth >= depth_limit, else #{k >= 1 : r < T[k-1]} with T from
+ * hs_uts_geo_table (geometric, mean `branching`).  Work stealing over per-CTA
+ * lock-free queues; the node count is exact. */
+typedef struct hs_uts_geo_result {
+  unsigned long long nodes, leaves;
+  unsigned max_depth;
+  float elapsed_ms;
+  unsigned dev_error_bits;
+} hs_uts_geo_result;
+const char* hs_uts_geo_last_error(void);
+/* T[k-1] = floor(2^31 q^k), q = b / (1 + b), q^k formed by repeated IEEE double
+ * multiplication; returns the number of nonzero entries. */
+int hs_uts_geo_table(double branching, uint32_t* table, int n);
+int hs_uts_geo_run(unsigned seed, int depth_limit, double branching, int blocks, int threads,
+                   unsigned long long timeout_ns, hs_uts_geo_result* r);
+
 /* ---- tree barrier with local exchange on thread-block clusters ----------------- */
 /* The LocalExch tree barriers (main.cu:153-270; joinBarrier_helper,
  * cudaLocksBarrierAtomic.cu:147-172; joinLFBarrier_helper,

@@ -9,6 +9,9 @@ the product (heterosync_gb300/) imports, links or runs anything from here.
   twins.cpp  std::thread / std::atomic runs of the same lock, semaphore and
              barrier algorithms (the host-thread CPU baseline)
   uts.c      the UTS binary-tree generator and its golden (cuda/uts/uvm/uts.cu:290-339)
+  uts_geo.c  geometric UTS tree with a SHA-1 node generator, counted depth-first
+             (no reference implementation: parity unpinned; SHA-1 checked
+             against hashlib)
 """
 from __future__ import annotations
 
@@ -172,3 +175,44 @@ def exchange_expected(buffers: np.ndarray, episodes: int) -> np.ndarray:
     holds the initial buffer of CTA (b - episodes) mod n."""
     n = buffers.shape[0]
     return np.roll(buffers, episodes % n if n else 0, axis=0)
+
+
+# Geometric SHA-1 UTS (uts_geo.c).
+def sha1(msg: bytes) -> bytes:
+    assert len(msg) <= 55
+    out = ctypes.create_string_buffer(20)
+    lib().hs_oracle_sha1.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_void_p]
+    lib().hs_oracle_sha1(msg, len(msg), out)
+    return out.raw
+
+
+def geo_table(b: float, n: int = 128):
+    t = np.zeros(n, dtype=np.uint32)
+    lib().hs_oracle_geo_table.argtypes = [ctypes.c_double, ctypes.c_void_p, ctypes.c_int]
+    nz = lib().hs_oracle_geo_table(b, t.ctypes.data, n)
+    return t, nz
+
+
+def geo_root(seed: int) -> bytes:
+    out = ctypes.create_string_buffer(20)
+    lib().hs_oracle_geo_root.argtypes = [ctypes.c_uint32, ctypes.c_void_p]
+    lib().hs_oracle_geo_root(seed, out)
+    return out.raw
+
+
+def geo_child(parent: bytes, i: int) -> bytes:
+    out = ctypes.create_string_buffer(20)
+    lib().hs_oracle_geo_child.argtypes = [ctypes.c_char_p, ctypes.c_uint32, ctypes.c_void_p]
+    lib().hs_oracle_geo_child(parent, i, out)
+    return out.raw
+
+
+def geo_count(seed: int, depth_limit: int, b: float = 4.0):
+    """(nodes, leaves, deepest level) of the geometric tree."""
+    n, lv, md = ctypes.c_ulonglong(), ctypes.c_ulonglong(), ctypes.c_int()
+    lib().hs_oracle_geo_count.argtypes = [ctypes.c_uint32, ctypes.c_int, ctypes.c_double, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_void_p]
+    rc = lib().hs_oracle_geo_count(seed, depth_limit, b, ctypes.byref(n), ctypes.byref(lv), ctypes.byref(md))
+    if rc:
+        raise ValueError("bad geometric tree parameters")
+    return n.value, lv.value, md.value
