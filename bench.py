@@ -66,6 +66,15 @@ TB_MULT = (1, 2, 4)
 SEED = 20260101
 
 
+# DRAM bytes (read + write) of one launch of the dominant sweep kernel, from
+# one ncu capture (spinSem1, 152 TBs x 256 threads, numLdSt 100): the chunk and
+# the lock word stay L2-resident, so DRAM traffic is the cold first read and
+# does not grow with the launch's operations.
+DRAM_BYTES_PER_LAUNCH = 120000
+TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_sem (spinSem1, 152 TBs, numLdSt 100); "
+                  "profiles/k_sem_spinSem1_152tbs_L100.md")
+
+
 def sweep_points(nsm):
     return [(m * nsm, L) for m in TB_MULT for L in LDST]
 
@@ -481,7 +490,8 @@ def main():
                     "d2h_bytes_per_step": int(sum(r["bytes"] for r in recs) / args.steps)},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
-                         "frac": achieved / peak_gbs, "peak_source": peak_kind, "traffic": None,
+                         "frac": achieved / peak_gbs, "peak_source": peak_kind, "traffic": DRAM_BYTES_PER_LAUNCH,
+                         "traffic_source": TRAFFIC_SOURCE,
                          "note": "critical-section bytes; these kernels are latency-bound (lock hand-off), see "
                                  "l2_atomic"},
             "l2_atomic": {"achieved": atom_achieved, "peak": atom_peak,
