@@ -22,7 +22,8 @@ barrier with local exchange on thread-block clusters: 592 CTAs, fp32[4096] per
 CTA rotated every episode, 1000 episodes, cluster sizes 1/2/4/8) and "batch"
 (the 64-instance mixed batch, one launch per instance against the autotuned
 persistent graph-replayed launch) and "serve" (the served request loop: peak
-request rate, p50/p99 latency under Poisson arrivals at 10-90% of it); the
+request rate, p50/p99 latency under Poisson arrivals at 10-90% of it) and
+"uts_geo" (geometric SHA-1 UTS, depth 12, nodes/s); the
 extras run outside the sweep's timed region; --no-extras skips them.
 
 --impl reference runs the reference's own SyncPrims kernels (built from its
@@ -302,6 +303,29 @@ def batch_extra(hs):
                      "tuned_on": "numCSIters / 25 (%.1f ms)" % tune_ms}}
 
 
+def uts_geo_extra(hs):
+    """Geometric SHA-1 UTS (branching 4, depth limit 12) counted by work
+    stealing on the GPU; node count checked against the host walk of the same
+    tree at depth 9 (bounded CPU sample, also the host rate)."""
+    import oracle
+    rows = {}
+    for seed in (2, 3):
+        n, lv, md, ms = hs.uts_geo_run(seed, 12, 4.0, blocks=304, threads=256)
+        rows["seed%d" % seed] = {"nodes": n, "leaves": lv, "deepest": md, "ms": round(ms, 3),
+                                 "nodes_per_s": n / (ms * 1e-3)}
+    want = oracle.geo_count(2, 9)
+    got = hs.uts_geo_run(2, 9, 4.0, blocks=304, threads=256)[:3]
+    if got != want:
+        raise SystemExit("bench: geometric UTS depth 9 count differs from the host walk")
+    t0 = time.perf_counter()
+    oracle.geo_count(2, 9)
+    host_s = time.perf_counter() - t0
+    return {"workload": "geometric tree, SHA-1 node generator, branching 4, depth limit 12, 304 CTAs x 256",
+            "results": rows, "check": "depth 9, seed 2: %d nodes, equal to the host walk" % want[0],
+            "cpu_baseline": {"nodes_per_s": want[0] / host_s, "cores": 1, "kind": "port",
+                             "sample": "host depth-first walk of seed 2 at depth 9 (%d nodes)" % want[0]}}
+
+
 def serve_extra(hs):
     """Served request loop: 256 requests from the mixed-instance generator
     (numCSIters / 50), 64 slots of 8-CTA clusters; peak request rate, then
@@ -508,7 +532,8 @@ def main():
         if ck:
             out["clocks"] = ck
         if not args.no_extras and world == 1:
-            for key, fn in (("exchange", exchange_extra), ("batch", batch_extra), ("serve", serve_extra)):
+            for key, fn in (("exchange", exchange_extra), ("batch", batch_extra), ("serve", serve_extra),
+                            ("uts_geo", uts_geo_extra)):
                 try:
                     out[key] = fn(hs)
                 except SystemExit:
