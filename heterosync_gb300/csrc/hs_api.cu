@@ -14,7 +14,7 @@
 
 namespace hs {
 using KernelFn = void (*)(RunDesc);
-KernelFn syncprim_plan(int prim, int mode, int threads, int num_ldst, size_t* smem_bytes);
+KernelFn syncprim_plan(int prim, int mode, int threads, int num_ldst, size_t* smem_bytes, bool bulk = true);
 cudaError_t prepare_smem(KernelFn fn, size_t smem_bytes);
 cudaError_t launch_ring_init(unsigned* ring, unsigned slots_per_group, unsigned groups, cudaStream_t st);
 cudaError_t launch_fill_lines(unsigned* base, size_t n, size_t stride, unsigned value, cudaStream_t st);
@@ -450,16 +450,40 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c, void* storage, int on
   const size_t bytes = words * 4;
 
   size_t smem = 0;
-  KernelFn fn = syncprim_plan(c->prim, c->mode, c->threads, c->num_ldst, &smem);
+  KernelFn fn = syncprim_plan(c->prim, c->mode, c->threads, c->num_ldst, &smem, !(c->flags & HS_RUN_REGISTER_CS));
   if (!fn) { g_err = "no kernel for this primitive/mode"; return r->status = HS_EINVAL; }
   HS_CK(prepare_smem(fn, smem));
+  // Tree barriers whose logical-SM groups are all the same size (numTBs a
+  // multiple of NUM_SM, 2 to 8 per group) run each group as one thread-block
+  // cluster: the local stage becomes the hardware cluster barrier.
+  int cluster = 1;
   if (is_barrier(c->prim)) {
-    int per_sm = 0;
-    HS_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, c->threads, 0));
-    if ((long long)per_sm * ctx->nsm < c->num_tbs) {
-      g_err = "barrier TBs cannot all be co-resident (" + std::to_string(per_sm) + " per SM x " +
-              std::to_string(ctx->nsm) + " SMs < " + std::to_string(c->num_tbs) + ")";
-      return r->status = HS_ENORES;
+    const int nb = c->num_tbs < nsm ? c->num_tbs : nsm;
+    const int m = c->num_tbs / nb;
+    if (!(c->flags & HS_RUN_NO_CLUSTER) && c->skip_tb < 0 && c->num_tbs % nb == 0 && (m == 2 || m == 4 || m == 8)) {
+      cudaLaunchConfig_t lc = {};
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = (unsigned)m;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      lc.gridDim = dim3((unsigned)c->num_tbs);
+      lc.blockDim = dim3((unsigned)c->threads);
+      lc.dynamicSmemBytes = smem;
+      lc.attrs = attr;
+      lc.numAttrs = 1;
+      int fit = 0;
+      if (cudaOccupancyMaxActiveClusters(&fit, (const void*)fn, &lc) == cudaSuccess && fit >= nb) cluster = m;
+      cudaGetLastError();
+    }
+    if (cluster == 1) {
+      int per_sm = 0;
+      HS_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, c->threads, smem));
+      if ((long long)per_sm * ctx->nsm < c->num_tbs) {
+        g_err = "barrier TBs cannot all be co-resident (" + std::to_string(per_sm) + " per SM x " +
+                std::to_string(ctx->nsm) + " SMs < " + std::to_string(c->num_tbs) + ")";
+        return r->status = HS_ENORES;
+      }
     }
   }
 
@@ -474,10 +498,24 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c, void* storage, int on
   RunDesc d;
   if ((s = hs_prepare_run(ctx, c, nsm, dev, st, &d, !(c->flags & HS_RUN_KEEP_STATE)))) return r->status = s;
 
+  d.cluster = cluster;
+  r->cluster = cluster;
+  cudaLaunchConfig_t lc = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  lc.gridDim = dim3((unsigned)c->num_tbs);
+  lc.blockDim = dim3((unsigned)c->threads);
+  lc.dynamicSmemBytes = smem;
+  lc.stream = st;
+  lc.attrs = attr;
+  lc.numAttrs = cluster > 1 ? 1 : 0;
   HS_CK(cudaEventRecord(ctx->ev[0], st));
   for (int rep = 0; rep < c->repeats; ++rep) {
     void* args[] = {&d};
-    HS_CK(cudaLaunchKernel((const void*)fn, dim3(c->num_tbs), dim3(c->threads), args, smem, st));
+    HS_CK(cudaLaunchKernelExC(&lc, (const void*)fn, args));
     r->launches++;
     if (c->flags & HS_RUN_SYNC_EACH) HS_CK(cudaStreamSynchronize(st));
   }

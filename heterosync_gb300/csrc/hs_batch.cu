@@ -35,7 +35,7 @@ int hs_layout_for(const hs_run_config* c, int nsm, hs::Layout* out);
 
 namespace hs {
 using KernelFn = void (*)(RunDesc);
-KernelFn syncprim_plan(int prim, int mode, int threads, int num_ldst, size_t* smem_bytes);
+KernelFn syncprim_plan(int prim, int mode, int threads, int num_ldst, size_t* smem_bytes, bool bulk = true);
 cudaError_t prepare_smem(KernelFn fn, size_t smem_bytes);
 cudaError_t launch_ring_init(unsigned* ring, unsigned slots_per_group, unsigned groups, cudaStream_t st);
 cudaError_t launch_fill_lines(unsigned* base, size_t n, size_t stride, unsigned value, cudaStream_t st);

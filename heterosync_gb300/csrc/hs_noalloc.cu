@@ -32,7 +32,7 @@
 
 namespace hs {
 using KernelFn = void (*)(RunDesc);
-KernelFn syncprim_plan(int prim, int mode, int threads, int num_ldst, size_t* smem_bytes);
+KernelFn syncprim_plan(int prim, int mode, int threads, int num_ldst, size_t* smem_bytes, bool bulk = true);
 cudaError_t prepare_smem(KernelFn fn, size_t smem_bytes);
 cudaError_t launch_ring_init(unsigned* ring, unsigned slots_per_group, unsigned groups, cudaStream_t st);
 cudaError_t launch_fill_lines(unsigned* base, size_t n, size_t stride, unsigned value, cudaStream_t st);
@@ -80,6 +80,7 @@ extern "C" int hs_run_noalloc(const hs_run_config* c, void* storage, void* strea
   using namespace hs;
   if (!c || !storage || !r) { set_err("null argument"); return HS_EINVAL; }
   std::memset(r, 0, sizeof(*r));
+  r->cluster = 1;
   int dev = 0, nsm = c->nsm;
   if (cudaGetDevice(&dev) != cudaSuccess) return r->status = HS_ECUDA;
   if (nsm <= 0 && cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)

@@ -17,6 +17,7 @@
 //  * barrier state is generation-valued (no resets) and groups may be uneven;
 //  * every wait is bounded (see hs_device.cuh).
 #include <cuda_runtime.h>
+#include <cstdlib>
 #include "hs_cs.cuh"
 
 namespace hs {
@@ -225,15 +226,83 @@ __device__ __forceinline__ bool tree_barrier(const RunDesc& d, int g, int r, int
   }
 }
 
+__device__ __forceinline__ unsigned dyn_smem_bytes_b() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%dynamic_smem_size;" : "=r"(r));
+  return r;
+}
+
+// Tree barrier with the local stage on a thread-block cluster: the group's
+// members are the cluster's CTAs.  Local arrival and local release are the
+// hardware cluster barrier; between them the leader (rank 0) runs the global
+// stage among the nb group leaders (generation counter, or flags scanned by
+// group 0's leader and one release word).  The leader's outcome goes to its
+// members through the group's spare line, written before the release barrier
+// and read after it, so every CTA of the cluster continues or stops together.
+template <bool LF>
+__device__ __forceinline__ bool cluster_tree_barrier(const RunDesc& d, int g, int r, int nb, BarState& s,
+                                                     const HsEnv& env) {
+  cluster_sync_all();  // local arrival: every member's stores are released at cluster scope
+  if (r == 0) {
+    unsigned* gcount = d.locks + (size_t)(d.l_glob + 0) * kLineWords;
+    unsigned* ggenw = d.locks + (size_t)(d.l_glob + 1) * kLineWords;
+    unsigned* ggo = d.locks + (size_t)(d.l_glob + 2) * kLineWords;
+    unsigned* gflags = d.locks + (size_t)d.l_gflag * kLineWords;
+    int ok = 1;
+    if constexpr (!LF) {
+      if (is_master()) {
+        bool okb = true;
+        counter_barrier<GPU>(gcount, ggenw, (unsigned)nb, s.ggen, d.bo_unit, env, HS_SITE_BAR_GLOBAL,
+                             [] { return true; }, &okb);
+        ok = okb;
+      }
+      ok = __syncthreads_or(!ok) == 0;
+    } else {
+      const unsigned E = s.ggen + 1u;
+      if (is_master()) st_release<GPU>(gflags + g, E);
+      if (g == 0) {
+        ok = scan_flags<GPU>(gflags, (unsigned)nb, E, d.bo_unit, env, HS_SITE_BAR_SCAN);
+        if (ok && is_master()) st_release<GPU>(ggo, E);
+      } else {
+        if (is_master())
+          ok = wait_until([&] { return (int)(ld_acquire<GPU>(ggo) - E) >= 0; }, [&] { sleep_ns(d.bo_unit); }, env,
+                          HS_SITE_BAR_GO);
+        ok = __syncthreads_or(!ok) == 0;
+      }
+    }
+    if (is_master()) st_relaxed<GPU>(group_line(d, g, 3), ok ? 0u : 1u);
+  }
+  cluster_sync_all();  // local release
+  s.ggen += 1u;
+  return ld_relaxed<GPU>(group_line(d, g, 3)) == 0u;
+}
+
 // Barrier TBs must all be co-resident, so the kernel is held to 64 registers
-// (four 256-thread TBs, 1024 threads, per SM).
-template <bool LF, bool EXCH, int MODE, int V>
-__global__ void __launch_bounds__(Bounds<V>::kThreads, 1024 / Bounds<V>::kThreads) k_barrier(RunDesc d) {
-  const int b = blockIdx.x;
+// (four 256-thread TBs, 1024 threads, per SM).  With d.cluster = m > 1 the
+// launch has clusters of m CTAs and numTBs = m * nb: physical CTA p runs
+// logical TB g + r * nb with g = p / m, r = p % m, so each logical-SM group is
+// one cluster (which physical CTA runs which logical TB does not change the
+// result: the data a TB touches depends only on its logical index).
+template <bool LF, bool EXCH, int MODE, int V, bool TMA = false>
+__global__ void __launch_bounds__(TMA ? 256 : Bounds<V>::kThreads, TMA ? 4 : 1024 / Bounds<V>::kThreads)
+    k_barrier(RunDesc d) {
+  // TMA: the critical section is staged through the launch's dynamic shared
+  // memory a tile of regions at a time (bulk copies); a bulk-copy wait that
+  // runs out records the failure in the status word, which every barrier
+  // wait sees, so all CTAs leave at the same barrier.
+  extern __shared__ __align__(128) unsigned char bar_smem[];
+  __shared__ unsigned long long s_bar_mbar;
+  TmaCtx tma;
+  if constexpr (TMA) {
+    tma_init(tma, &s_bar_mbar, bar_smem);
+    tma.cap = dyn_smem_bytes_b();
+  }
   const int Gd = d.num_tbs;
   const int nb = Gd < d.nsm ? Gd : d.nsm;
-  const int g = b % nb;
-  const int r = b / nb;
+  const bool clustered = d.cluster > 1;
+  const int g = clustered ? (int)blockIdx.x / d.cluster : (int)blockIdx.x % nb;
+  const int r = clustered ? (int)blockIdx.x % d.cluster : (int)blockIdx.x / nb;
+  const int b = g + r * nb;
   const int m = (Gd - g + nb - 1) / nb;
   const int kmax = ceil_div(Gd, nb);
   const HsEnv env{d.status, d.timeout_ns};
@@ -255,13 +324,16 @@ __global__ void __launch_bounds__(Bounds<V>::kThreads, 1024 / Bounds<V>::kThread
     // numBlocksAtBarr TBs ahead (one call site keeps one inlined copy of the CS)
     for (int ph = 0; ph < phases; ++ph) {
       if (ph == 1) {
-        if (!local_only_barrier<LF>(d, g, r, m, s, env)) return;
+        if (clustered) cluster_sync_all();
+        else if (!local_only_barrier<LF>(d, g, r, m, s, env)) return;
         cur = (cur + nb) % Gd;
       }
-      cs_chunk<MODE, V>(d, cur);
-      if (b == d.skip_tb) return;  // fault injection: this TB never arrives
+      if constexpr (TMA) cs_chunk_tma_tiled<MODE>(d, cur, tma, tma.cap, env);
+      else cs_chunk<MODE, V>(d, cur);
+      if (b == d.skip_tb) return;  // fault injection: this TB never arrives (never in cluster mode)
     }
-    if (!tree_barrier<LF>(d, g, r, m, nb, s, env)) return;
+    if (clustered ? !cluster_tree_barrier<LF>(d, g, r, nb, s, env) : !tree_barrier<LF>(d, g, r, m, nb, s, env))
+      return;
     cur = (cur + 1) % Gd;
   }
 }
@@ -284,14 +356,12 @@ using KernelFn = void (*)(RunDesc);
 template <int MODE, int V, bool TMA>
 static KernelFn pick(int prim) {
   if constexpr (MODE != M_SLICE) {
-    if constexpr (!TMA) {  // barriers need all TBs co-resident: register path only
-      switch (prim) {
-        case P_ATOMIC_TREE: return k_barrier<false, false, MODE, V>;
-        case P_ATOMIC_TREE_EXCH: return k_barrier<false, true, MODE, V>;
-        case P_LF_TREE: return k_barrier<true, false, MODE, V>;
-        case P_LF_TREE_EXCH: return k_barrier<true, true, MODE, V>;
-        default: break;
-      }
+    switch (prim) {
+      case P_ATOMIC_TREE: return k_barrier<false, false, MODE, V, TMA>;
+      case P_ATOMIC_TREE_EXCH: return k_barrier<false, true, MODE, V, TMA>;
+      case P_LF_TREE: return k_barrier<true, false, MODE, V, TMA>;
+      case P_LF_TREE_EXCH: return k_barrier<true, true, MODE, V, TMA>;
+      default: break;
     }
     if (prim >= P_SPIN_SEM1 && prim <= P_SPIN_SEM120) return k_sem<false, false, MODE, V, TMA>;
     if (prim >= P_EBO_SEM1 && prim <= P_EBO_SEM120) return k_sem<true, false, MODE, V, TMA>;
@@ -336,13 +406,18 @@ static KernelFn pick_v(int prim, int mode) {
 // Kernel choice for a run.  Mutex and semaphore kernels with numLdSt > 32 whose
 // chunk fits in shared memory take the TMA path (dynamic shared memory = one
 // chunk); otherwise the register path with the deepest vector variant the
-// thread count allows.  Barrier kernels always take the register path (all TBs
-// must be co-resident).
-KernelFn syncprim_plan(int prim, int mode, int threads, int num_ldst, size_t* smem_bytes) {
+// thread count allows.  Barrier kernels (every TB co-resident, four 256-thread
+// TBs per SM) with numLdSt > 32 stage their chunks through 48 KB tiles.
+constexpr size_t kBarrierStageBytes = 48u * 1024u;
+KernelFn syncprim_plan(int prim, int mode, int threads, int num_ldst, size_t* smem_bytes, bool bulk = true) {
   const bool barrier = prim >= P_ATOMIC_TREE && prim <= P_LF_TREE_EXCH;
   const size_t chunk = (size_t)threads * (num_ldst + 1) * 4;
   *smem_bytes = 0;
-  if (!barrier && mode != M_SLICE && threads <= 256 && num_ldst > 32 && chunk <= kTmaMaxBytes) {
+  if (bulk && barrier && mode != M_SLICE && threads <= 256 && num_ldst > 32) {
+    *smem_bytes = chunk < kBarrierStageBytes ? chunk : kBarrierStageBytes;
+    return pick_v<8, true>(prim, mode);
+  }
+  if (bulk && !barrier && mode != M_SLICE && threads <= 256 && num_ldst > 32 && chunk <= kTmaMaxBytes) {
     *smem_bytes = chunk;
     return pick_v<8, true>(prim, mode);
   }
@@ -357,7 +432,7 @@ KernelFn syncprim_kernel(int prim, int mode, int threads, int num_ldst) {
 
 // Allow the kernel its dynamic shared memory (once per function).
 cudaError_t prepare_smem(KernelFn fn, size_t smem_bytes) {
-  if (smem_bytes <= 48 * 1024) return cudaSuccess;
+  if (smem_bytes <= 32 * 1024) return cudaSuccess;  // dynamic + static must stay under the 48 KB default
   return cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTmaMaxBytes);
 }
 

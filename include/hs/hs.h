@@ -45,7 +45,9 @@ enum {
 /* ---- run flags --------------------------------------------------------------- */
 enum {
   HS_RUN_SYNC_EACH = 1,   /* host-synchronise after every launch, as main.cu:844-854 does */
-  HS_RUN_KEEP_STATE = 2   /* do not re-initialise lock state before the repeats */
+  HS_RUN_KEEP_STATE = 2,  /* do not re-initialise lock state before the repeats */
+  HS_RUN_NO_CLUSTER = 4,  /* tree barriers: keep the local stage in L2 instead of on thread-block clusters */
+  HS_RUN_REGISTER_CS = 8  /* critical sections on the register path only (no bulk copies through shared memory) */
 };
 
 /* One run of one SyncPrims primitive: `repeats` launches of `num_tbs` TBs of
@@ -76,6 +78,7 @@ typedef struct hs_run_result {
   float h2d_ms, d2h_ms;         /* storage copies when storage is host memory */
   unsigned long long ops;       /* num_tbs * num_iters * repeats */
   unsigned launches;            /* kernels launched by this call */
+  int cluster;                  /* tree barriers: CTAs per thread-block cluster (1: no clusters) */
 } hs_run_result;
 
 typedef struct hs_ctx hs_ctx;

@@ -114,3 +114,31 @@ def test_uneven_barrier_groups_complete(hs, oracle):
         hs.run(cfg, st)
         want = oracle.golden(prim, 32, 20, 11, 3, 2, 4, True, init)
         assert np.array_equal(st, want)
+
+
+@pytest.mark.parametrize("prim", [0, 1, 2, 3])
+@pytest.mark.parametrize("mult", [2, 4])
+@pytest.mark.parametrize("L", [10, 64])
+def test_barrier_groups_on_clusters(hs, oracle, prim, mult, L):
+    """numTBs = mult * NUM_SM: each logical-SM group runs as one thread-block
+    cluster (local stage = hardware cluster barrier); the result equals the
+    flat launch's and the golden's, on the register path (numLdSt 10) and the
+    tiled bulk-copy path (numLdSt 64)."""
+    nsm = hs.device_info()["nsm"]
+    G = mult * nsm
+    outs = []
+    for flags in (0, hs.RUN_NO_CLUSTER):
+        cfg = hs.RunConfig(prim=prim, num_ldst=L, num_tbs=G, num_iters=4, threads=256, repeats=2, mode="inc",
+                           flags=flags, timeout_ns=5_000_000_000)
+        init = _init(hs.storage_words(cfg), prim + 7 * mult)
+        st = init.copy()
+        res = hs.run(cfg, st)
+        # clusters of `mult` are used when numTBs / mult of them can be resident
+        # (at 4 per SM the GPCs do not hold every cluster of 4: flat launch)
+        assert res.status == 0 and res.cluster in ((mult, 1) if flags == 0 else (1,))
+        if mult == 2 and flags == 0:
+            assert res.cluster == 2
+        assert np.array_equal(st, hs.expected_storage(cfg, init))
+        outs.append(st)
+    want = oracle.golden(prim, 256, L, G, 4, 2, nsm, True, init)
+    assert np.array_equal(outs[0], want) and np.array_equal(outs[1], want)
