@@ -143,18 +143,12 @@ __device__ __forceinline__ bool local_only_barrier(const RunDesc& d, int g, int 
     s.lgen += 1u;
     return __syncthreads_or(!ok) == 0;  // non-masters keep ok == 1
   } else {
+    // every member publishes its flag and scans the group's flags itself: one
+    // hop, no leader release (the flags share one line)
+    (void)lgo;
     const unsigned e = s.lgen + 1u;
-    if (r != 0) {
-      if (is_master()) {
-        st_release<GPU>(lflags + r, e);
-        ok = wait_until([&] { return (int)(ld_acquire<GPU>(lgo) - e) >= 0; }, [&] { sleep_ns(d.bo_unit); }, env,
-                        HS_SITE_BAR_GO);
-      }
-      ok = __syncthreads_or(!ok) == 0;
-    } else {
-      ok = scan_flags<GPU>(lflags + 1, (unsigned)(m - 1), e, d.bo_unit, env, HS_SITE_BAR_SCAN);
-      if (ok && is_master()) st_release<GPU>(lgo, e);
-    }
+    if (is_master()) st_release<GPU>(lflags + r, e);
+    ok = scan_flags<GPU>(lflags, (unsigned)m, e, d.bo_unit, env, HS_SITE_BAR_SCAN);
     s.lgen = e;
     return ok != 0;
   }
@@ -196,19 +190,25 @@ __device__ __forceinline__ bool tree_barrier(const RunDesc& d, int g, int r, int
     s.ggen += 1u;
     return __syncthreads_or(!ok) == 0;
   } else {
+    // Members publish their flag and wait for the global release word
+    // directly; the leader scans its group's flags, publishes the group's
+    // flag, and group 0's leader scans those and releases.  The global release
+    // implies every group's arrival, so members need no local release hop.
     const unsigned e = s.lgen + 1u;
     const unsigned E = s.ggen + 1u;
-    unsigned* lgo = group_line(d, g, 2);
     unsigned* lflags = d.locks + (size_t)(d.l_lflag + g * d.lflag_lines) * kLineWords;
     if (r != 0) {
       if (is_master()) {
         st_release<GPU>(lflags + r, e);
-        ok = wait_until([&] { return (int)(ld_acquire<GPU>(lgo) - e) >= 0; }, [&] { sleep_ns(d.bo_unit); }, env,
+        ok = wait_until([&] { return (int)(ld_acquire<GPU>(ggo) - E) >= 0; }, [&] { sleep_ns(d.bo_unit); }, env,
                         HS_SITE_BAR_GO);
       }
       ok = __syncthreads_or(!ok) == 0;
     } else {
-      if (m > 1) ok = scan_flags<GPU>(lflags + 1, (unsigned)(m - 1), e, d.bo_unit, env, HS_SITE_BAR_SCAN);
+      if (m > 1) {
+        if (is_master()) st_release<GPU>(lflags, e);
+        ok = scan_flags<GPU>(lflags + 1, (unsigned)(m - 1), e, d.bo_unit, env, HS_SITE_BAR_SCAN);
+      }
       if (ok && is_master()) st_release<GPU>(gflags + g, E);
       if (g == 0) {
         if (ok) ok = scan_flags<GPU>(gflags, (unsigned)nb, E, d.bo_unit, env, HS_SITE_BAR_SCAN);
@@ -217,7 +217,6 @@ __device__ __forceinline__ bool tree_barrier(const RunDesc& d, int g, int r, int
         ok = wait_until([&] { return (int)(ld_acquire<GPU>(ggo) - E) >= 0; }, [&] { sleep_ns(d.bo_unit); }, env,
                         HS_SITE_BAR_GO);
       }
-      if (is_master() && ok && m > 1) st_release<GPU>(lgo, e);
       ok = __syncthreads_or(!ok) == 0;
     }
     if (m > 1) s.lgen = e;
@@ -310,7 +309,9 @@ __global__ void __launch_bounds__(TMA ? 256 : Bounds<V>::kThreads, TMA ? 4 : 102
   // Generations at kernel start (state persists across launches).
   __shared__ BarState s_init;
   if (is_master()) {
-    s_init.lgen = LF ? ld_relaxed<GPU>(group_line(d, g, 2)) : ld_relaxed<GPU>(group_line(d, g, 1));
+    // LF: a member's own flag holds the group generation it last published
+    s_init.lgen = LF ? ld_relaxed<GPU>(d.locks + (size_t)(d.l_lflag + g * d.lflag_lines) * kLineWords + r)
+                     : ld_relaxed<GPU>(group_line(d, g, 1));
     s_init.ggen = LF ? ld_relaxed<GPU>(d.locks + (size_t)(d.l_glob + 2) * kLineWords)
                      : ld_relaxed<GPU>(d.locks + (size_t)(d.l_glob + 1) * kLineWords);
   }
