@@ -271,23 +271,22 @@ def batch_extra(hs):
     small = hs.batch_generate(seed=SEED, n=64, iter_div=25)
     tb = hs.Batch(small, mode="inc")
     _, tune_ms = tb.autotune()
-    cl, se, v, _ = tb.get_plan()
+    tuned = tb.tuned_settings()
     tb.close()
     b = hs.Batch(insts, mode="inc")
     rng = np.random.default_rng(SEED)
     inits = [rng.integers(0, 1000, size=b.words(i)).astype(np.uint32) for i in range(len(insts))]
 
     def check(tag):
-        for i, (p, L, G, I) in enumerate(insts):
-            cfg = hs.RunConfig(prim=p, num_ldst=L, num_tbs=G, num_iters=I, threads=THREADS, repeats=1, mode="inc")
-            if not np.array_equal(b.get_storage(i), hs.expected_storage(cfg, inits[i])):
+        for i, x in enumerate(insts):
+            if not np.array_equal(b.get_storage(i), hs.batch_expected(x, inits[i])):
                 raise SystemExit("bench: batch instance %d differs after the %s run" % (i, tag))
 
     for i, a in enumerate(inits):
         b.set_storage(i, a)
     rs = b.run_serial()
     check("per-launch")
-    s, grid, cap = b.plan_ex(cl, se, v)
+    s, grid, cap = b.apply_settings(tuned)
     if s:
         raise SystemExit("bench: the tuned batch plan does not fit (status %d)" % s)
     for i, a in enumerate(inits):
@@ -295,11 +294,13 @@ def batch_extra(hs):
     rb = b.run()
     check("batched")
     b.close()
-    return {"workload": "64 mixed SyncPrims instances (seed %d), numCSIters [10,5000]" % SEED,
+    return {"workload": "64 mixed instances (28 SyncPrims + RefCounter/SplitCounter/Seqlock/Flags, seed %d), "
+                        "numCSIters [10,5000]" % SEED,
             "ops": rb.ops, "per_launch_ms": round(rs.elapsed_ms, 2), "per_launch_ops_per_s": rs.ops / (rs.elapsed_ms * 1e-3),
             "launches_per_instance_form": rs.launches, "batched_ms": round(rb.elapsed_ms, 2),
             "batched_ops_per_s": rb.ops / (rb.elapsed_ms * 1e-3), "ratio": rs.elapsed_ms / rb.elapsed_ms,
-            "plan": {"cluster": cl, "serial_executors": se, "tbs_per_executor": v, "grid": grid, "capacity": cap,
+            "plan": {"cluster": tuned[0], "serial_executors": tuned[1], "tbs_per_executor": tuned[2],
+                     "stage_bytes": tuned[3], "backoff_max_ns": tuned[4], "grid": grid, "capacity": cap,
                      "tuned_on": "numCSIters / 25 (%.1f ms)" % tune_ms}}
 
 

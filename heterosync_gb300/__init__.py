@@ -622,8 +622,40 @@ class _BatchResult(ctypes.Structure):
                 ("failed_instance", ctypes.c_int)]
 
 
+BATCH_REFCOUNTER, BATCH_SPLITCOUNTER, BATCH_SEQLOCK, BATCH_FLAGS = 40, 41, 42, 43
+BATCH_KIND_NAMES = {40: "RefCounter", 41: "SplitCounter", 42: "Seqlock", 43: "Flags"}
+
+
+def batch_instance_words(inst, nsm: int = 0) -> int:
+    """Storage words of one (prim, num_ldst, num_tbs, num_iters) instance."""
+    nsm = nsm or device_info()["nsm"]
+    x = _BatchInst(*inst)
+    w = ctypes.c_size_t()
+    lib().hs_batch_instance_words.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    s = lib().hs_batch_instance_words(ctypes.byref(x), nsm, ctypes.byref(w))
+    if s:
+        raise HsError(s, "instance words")
+    return int(w.value)
+
+
+def batch_expected(inst, init, nsm: int = 0, mode: str = "inc"):
+    """Closed-form final storage of one batch or served instance (any kind)."""
+    np = _np()
+    nsm = nsm or device_info()["nsm"]
+    init = np.ascontiguousarray(init, dtype=np.uint32)
+    out = np.empty_like(init)
+    x = _BatchInst(*inst)
+    lib().hs_batch_expected_storage.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                                ctypes.c_void_p, ctypes.c_size_t]
+    s = lib().hs_batch_expected_storage(ctypes.byref(x), nsm, _MODES[mode], _p(init), _p(out), init.size)
+    if s:
+        raise HsError(s, "batch expected storage")
+    return out
+
+
 def batch_generate(seed: int, n: int = 64, nsm: int = 0, iter_div: int = 1):
-    """The BASELINE mixed batch: list of (prim, num_ldst, num_tbs, num_iters)."""
+    """The mixed batch: list of (prim, num_ldst, num_tbs, num_iters); prim is
+    a SyncPrims id or one of the BATCH_* relaxed-atomics kinds."""
     nsm = nsm or device_info()["nsm"]
     arr = (_BatchInst * n)()
     s = lib().hs_batch_generate(ctypes.c_ulonglong(seed), n, nsm, iter_div, arr)
@@ -697,6 +729,34 @@ class Batch:
         self._check(lib().hs_batch_get_plan(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
                                             ctypes.byref(d)))
         return a.value, b.value, c.value, d.value
+
+    def set_backoff(self, bo_min: int, bo_max: int):
+        """EBO bounds (ns) of the batched launch; invalidates the plan."""
+        lib().hs_batch_set_backoff.argtypes = [ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint]
+        self._check(lib().hs_batch_set_backoff(self.h, bo_min, bo_max))
+
+    def get_backoff(self):
+        a, b = ctypes.c_uint(), ctypes.c_uint()
+        lib().hs_batch_get_backoff.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        self._check(lib().hs_batch_get_backoff(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def get_stage(self) -> int:
+        lib().hs_batch_get_stage.argtypes = [ctypes.c_void_p]
+        lib().hs_batch_get_stage.restype = ctypes.c_uint
+        return int(lib().hs_batch_get_stage(self.h))
+
+    def tuned_settings(self):
+        """(cluster, serial executors, v, staging bytes, backoff cap) of the current plan."""
+        cl, se, v, _ = self.get_plan()
+        return cl, se, v, self.get_stage(), self.get_backoff()[1]
+
+    def apply_settings(self, settings):
+        """Apply tuned_settings() of another batch (e.g. one tuned on fewer iterations)."""
+        cl, se, v, stage, bo = settings
+        self.set_stage(stage)
+        self.set_backoff(1, bo)
+        return self.plan_ex(cl, se, v)
 
     def set_stage(self, nbytes: int):
         """Staging bytes per CTA (0 = whole chunks); invalidates the plan."""

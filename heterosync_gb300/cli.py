@@ -25,7 +25,7 @@ import sys
 
 import numpy as np
 
-from . import (Batch, RunConfig, batch_generate, exchange_fill, exchange_run, expected_storage)
+from . import (Batch, batch_expected, batch_generate, exchange_fill, exchange_run)
 
 
 def _rotation(x, episodes):
@@ -47,22 +47,20 @@ def cmd_batch(a):
     insts = batch_generate(seed=a.seed, n=a.n, iter_div=a.iter_div)
     tb = Batch(batch_generate(seed=a.seed, n=a.n, iter_div=a.tune_div), mode="inc")
     tb.autotune()
-    cl, se, v, _ = tb.get_plan()
+    tuned = tb.tuned_settings()
     tb.close()
     b = Batch(insts, mode="inc")
     rng = np.random.default_rng(a.seed)
     inits = [rng.integers(0, 1000, size=b.words(i)).astype(np.uint32) for i in range(len(insts))]
 
     def exact():
-        return all(np.array_equal(b.get_storage(i), expected_storage(
-            RunConfig(prim=p, num_ldst=L, num_tbs=G, num_iters=I, threads=256, repeats=1, mode="inc"), inits[i]))
-            for i, (p, L, G, I) in enumerate(insts))
+        return all(np.array_equal(b.get_storage(i), batch_expected(x, inits[i])) for i, x in enumerate(insts))
 
     for i, x in enumerate(inits):
         b.set_storage(i, x)
     rs = b.run_serial()
     ok_serial = exact()
-    b.plan_ex(cl, se, v)
+    b.apply_settings(tuned)
     for i, x in enumerate(inits):
         b.set_storage(i, x)
     rb = b.run()
@@ -70,7 +68,9 @@ def cmd_batch(a):
     b.close()
     print(json.dumps({"workload": "batch", "instances": len(insts), "ops": rb.ops,
                       "per_launch_ms": rs.elapsed_ms, "batched_ms": rb.elapsed_ms,
-                      "ratio": rs.elapsed_ms / rb.elapsed_ms, "plan": [cl, se, v], "grid": rb.grid,
+                      "ratio": rs.elapsed_ms / rb.elapsed_ms,
+                      "plan": dict(zip(["cluster", "serial_executors", "tbs_per_executor", "stage_bytes", "backoff_max_ns"],
+                                       tuned)), "grid": rb.grid,
                       "bit_exact": ok_serial and ok_batch}), flush=True)
     return 0 if ok_serial and ok_batch else 1
 

@@ -81,7 +81,11 @@ __global__ void __launch_bounds__(256, 4) k_batch(const BatchInst* insts, int n_
   const int rank = cta - bi.first_cta, c = bi.gang;
   const HsEnv env{d.status, d.timeout_ns};
   if (rank >= 0 && rank < c) {
-    if (is_mutex_prim(d.prim) || is_sem_prim(d.prim)) {
+    if (is_relaxed_prim(d.prim)) {
+      bool ok = true;
+      for (int j = 0; j < d.iters && ok; ++j)
+        for (int b = rank; b < d.num_tbs && ok; b += c) ok = relaxed_op(d, b, j, env);
+    } else if (is_mutex_prim(d.prim) || is_sem_prim(d.prim)) {
       // one executor per ecl CTAs (a whole cluster, or one CTA); executor x
       // runs the logical TBs congruent to x
       const int ecl = bi.ecl, er = ecl == 1 ? 0 : cr;
@@ -98,6 +102,13 @@ __global__ void __launch_bounds__(256, 4) k_batch(const BatchInst* insts, int n_
   }
   // no CTA of a cluster may exit while another rank can still read its shared memory
   cl_barrier(cl);
+}
+
+// One standalone launch of a relaxed-atomics instance: CTA b is logical TB b.
+__global__ void __launch_bounds__(256) k_relaxed_inst(RunDesc d) {
+  const HsEnv env{d.status, d.timeout_ns};
+  for (int j = 0; j < d.iters; ++j)
+    if (!relaxed_op(d, (int)blockIdx.x, j, env)) return;
 }
 
 }  // namespace hs
@@ -126,6 +137,7 @@ struct hs_batch {
   unsigned graph_kernels = 0;
   unsigned stage = kBatchBufSmall;  // staging bytes per CTA
   int cl = 1, serial_execs = 0;
+  unsigned bo_min = 1, bo_max = 1024;  // EBO bounds of the batched launch (the per-launch form keeps 1..1024)
   cudaEvent_t e0 = nullptr, e1 = nullptr;
 };
 
@@ -138,23 +150,118 @@ bool is_usem_p(int p) { return p >= 24 && p <= 31; }
 
 extern "C" const char* hs_batch_last_error(void) { return g_berr.c_str(); }
 
-// The BASELINE mixed batch: instances drawn from std::mt19937_64(seed) in the
-// order primitive, numTBs, numLdSt, numCSIters; u = (draw >> 11) * 2^-53.
-// primitive uniform over the 28 SyncPrims, numTBs = round(exp(U(ln 4, ln 512))),
+static bool relaxed_kind(int p) { return p >= HS_BATCH_REFCOUNTER && p <= HS_BATCH_FLAGS; }
+
+// Storage words of one instance (SyncPrims: the reference's storage; the
+// relaxed kinds: their counters, payload and data words).
+extern "C" int hs_batch_instance_words(const hs_batch_instance* x, int nsm, size_t* words) {
+  if (!x || !words || nsm <= 0 || x->num_tbs <= 0 || x->num_iters <= 0 || x->num_ldst <= 0) return HS_EINVAL;
+  switch (x->prim) {
+    case HS_BATCH_REFCOUNTER: *words = 2 * (size_t)x->num_ldst; return HS_OK;
+    case HS_BATCH_SPLITCOUNTER: *words = 2 * (size_t)nsm; return HS_OK;
+    case HS_BATCH_SEQLOCK: *words = 9; return HS_OK;
+    case HS_BATCH_FLAGS: *words = (size_t)x->num_ldst + 1; return HS_OK;
+    default: break;
+  }
+  hs_run_config c;
+  hs_run_config_default(&c);
+  c.prim = x->prim;
+  c.num_ldst = x->num_ldst;
+  c.num_tbs = x->num_tbs;
+  c.num_iters = x->num_iters;
+  c.threads = 256;
+  c.repeats = 1;
+  c.mode = HS_MODE_INC;
+  return hs_storage_words(&c, nsm, words);
+}
+
+static unsigned long long seq_pattern_host(unsigned seq, int i) {
+  return (unsigned long long)seq * 0x9E3779B97F4A7C15ull + (unsigned long long)i;
+}
+
+// Final storage of one instance after one run at 256 threads per TB, from its
+// initial storage (the closed forms of the operations in hs_exec.cuh).
+extern "C" int hs_batch_expected_storage(const hs_batch_instance* x, int nsm, int mode, const uint32_t* init,
+                                         uint32_t* out, size_t words) {
+  size_t need = 0;
+  int s = hs_batch_instance_words(x, nsm, &need);
+  if (s) return s;
+  if (!init || !out || words < need) return HS_EINVAL;
+  const int T = 256, L = x->num_ldst, G = x->num_tbs, I = x->num_iters;
+  std::memcpy(out, init, need * 4);
+  switch (x->prim) {
+    case HS_BATCH_REFCOUNTER: {
+      // total[k] += #{(b, j, t) : (b + j + t) mod L == k}
+      std::vector<unsigned long long> bj(L, 0), tt(L, 0);
+      for (long long v = 0; v <= (long long)G - 1 + I - 1; ++v) {
+        const long long lo_b = std::max(0LL, v - (I - 1)), hi_b = std::min((long long)G - 1, v);
+        if (hi_b >= lo_b) bj[v % L] += (unsigned long long)(hi_b - lo_b + 1);
+      }
+      for (int t = 0; t < T; ++t) tt[t % L] += 1;
+      for (int k = 0; k < L; ++k) {
+        unsigned long long n = 0;
+        for (int r = 0; r < L; ++r) n += bj[r] * tt[((k - r) % L + L) % L];
+        out[L + k] = init[L + k] + (uint32_t)n;
+      }
+      return HS_OK;
+    }
+    case HS_BATCH_SPLITCOUNTER: {
+      for (int sm = 0; sm < nsm; ++sm) {
+        const unsigned long long tbs = (unsigned long long)(G / nsm + (sm < G % nsm ? 1 : 0));
+        unsigned long long v = (unsigned long long)init[2 * sm] | ((unsigned long long)init[2 * sm + 1] << 32);
+        v += tbs * (unsigned long long)I * (unsigned long long)T * (unsigned long long)L;
+        out[2 * sm] = (uint32_t)v;
+        out[2 * sm + 1] = (uint32_t)(v >> 32);
+      }
+      return HS_OK;
+    }
+    case HS_BATCH_SEQLOCK: {
+      const unsigned writers = (unsigned)((G + 3) / 4);
+      const unsigned seq = 2u * writers * (unsigned)I;
+      for (int i = 0; i < 4; ++i) {
+        const unsigned long long p = seq_pattern_host(seq, i);
+        out[2 * i] = (uint32_t)p;
+        out[2 * i + 1] = (uint32_t)(p >> 32);
+      }
+      return HS_OK;  // torn-read count (word 8) unchanged
+    }
+    case HS_BATCH_FLAGS:
+      for (int k = 0; k < L; ++k) out[k] = (uint32_t)I;
+      return HS_OK;  // violation count (word L) unchanged
+    default: {
+      hs_run_config c;
+      hs_run_config_default(&c);
+      c.prim = x->prim;
+      c.num_ldst = L;
+      c.num_tbs = G;
+      c.num_iters = I;
+      c.threads = T;
+      c.repeats = 1;
+      c.mode = mode;
+      return hs_expected_storage(&c, nsm, init, out, words);
+    }
+  }
+}
+
+// The mixed batch: instances drawn from std::mt19937_64(seed) in the order
+// primitive, numTBs, numLdSt, numCSIters; u = (draw >> 11) * 2^-53.
+// primitive uniform over the 28 SyncPrims and the four relaxed-atomics kinds
+// (RefCounter, SplitCounter, Seqlock, Flags), numTBs = round(exp(U(ln 4, ln 512))),
 // numLdSt = 1 + floor(128 u), numCSIters = 10 + floor(4991 u) divided by
 // iter_div (>= 1).  Barrier and per-SM-semaphore instances with numTBs above
 // NUM_SM are rounded to a multiple of NUM_SM (the reference defines those only
 // for whole SM groups: README.txt:80, main.cu:1775-1786).
 extern "C" int hs_batch_generate(unsigned long long seed, int n, int nsm, int iter_div, hs_batch_instance* out) {
-  static const int prims[28] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15,
-                                20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30, 31};
+  static const int prims[32] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15,
+                                20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30, 31,
+                                HS_BATCH_REFCOUNTER, HS_BATCH_SPLITCOUNTER, HS_BATCH_SEQLOCK, HS_BATCH_FLAGS};
   if (n <= 0 || nsm <= 0 || !out) return HS_EINVAL;
   if (iter_div < 1) iter_div = 1;
   std::mt19937_64 rng(seed);
   auto u = [&] { return (double)(rng() >> 11) * (1.0 / 9007199254740992.0); };
   for (int i = 0; i < n; ++i) {
     hs_batch_instance& x = out[i];
-    x.prim = prims[std::min(27, (int)(u() * 28.0))];
+    x.prim = prims[std::min(31, (int)(u() * 32.0))];
     int G = (int)std::lround(std::exp(std::log(4.0) + u() * (std::log(512.0) - std::log(4.0))));
     if ((is_barrier_p(x.prim) || is_usem_p(x.prim)) && G > nsm) G = std::max(1, (int)std::lround((double)G / nsm)) * nsm;
     x.num_tbs = G;
@@ -190,10 +297,20 @@ extern "C" int hs_batch_create(const hs_batch_instance* inst, int n, int threads
     c.repeats = 1;
     c.mode = mode;
     size_t w = 0;
-    int s = hs_storage_words(&c, B->nsm, &w);
-    if (s) { g_berr = hs_last_error(); delete B; return s; }
     Layout L;
-    hs_layout_for(&c, B->nsm, &L);
+    if (relaxed_kind(c.prim)) {
+      int s = hs_batch_instance_words(&inst[i], B->nsm, &w);
+      if (s) { g_berr = "bad relaxed-atomics instance"; delete B; return s; }
+      std::memset(&L, 0, sizeof(L));
+      L.l_glob = 0;
+      L.l_grp = 4;  // line 4: seqlock sequence / flags word
+      L.groups = 1;
+      L.lines = 8;
+    } else {
+      int s = hs_storage_words(&c, B->nsm, &w);
+      if (s) { g_berr = hs_last_error(); delete B; return s; }
+      hs_layout_for(&c, B->nsm, &L);
+    }
     B->cfg.push_back(c);
     B->words.push_back(w);
     B->lay.push_back(L);
@@ -230,7 +347,7 @@ extern "C" int hs_batch_create(const hs_batch_instance* inst, int n, int threads
     d.num_tbs = c.num_tbs;
     d.iters = c.num_iters;
     d.nsm = B->nsm;
-    d.sem_max = (unsigned)hs_prim_sem_count(c.prim) + 1u;
+    d.sem_max = relaxed_kind(c.prim) ? 1u : (unsigned)hs_prim_sem_count(c.prim) + 1u;
     d.bo_min = 1;
     d.bo_max = 1024;
     d.bo_unit = 0;
@@ -409,6 +526,10 @@ extern "C" int hs_batch_plan_ex(hs_batch* B, int cl, int serial_execs, int v, in
   B->cl = cl;
   B->serial_execs = serial_execs;
   B->dev_order = B->host_desc;
+  for (auto& x : B->dev_order) {
+    x.d.bo_min = B->bo_min;
+    x.d.bo_max = B->bo_max;
+  }
   std::sort(B->dev_order.begin(), B->dev_order.end(),
             [](const BatchInst& x, const BatchInst& y) { return x.first_cta < y.first_cta; });
   if (cudaMemcpy(B->d_desc, B->dev_order.data(), sizeof(BatchInst) * B->n, cudaMemcpyHostToDevice) != cudaSuccess)
@@ -487,6 +608,11 @@ extern "C" int hs_batch_run_serial(hs_batch* B, void* stream, hs_batch_result* r
   std::vector<KernelFn> fns(B->n);
   std::vector<size_t> smem(B->n);
   for (int i = 0; i < B->n; ++i) {
+    if (relaxed_kind(B->cfg[i].prim)) {
+      fns[i] = k_relaxed_inst;
+      smem[i] = 0;
+      continue;
+    }
     fns[i] = syncprim_plan(B->cfg[i].prim, B->cfg[i].mode, B->threads, B->cfg[i].num_ldst, &smem[i]);
     if (!fns[i] || prepare_smem(fns[i], smem[i]) != cudaSuccess) { g_berr = "no kernel"; return HS_EINVAL; }
   }
@@ -525,9 +651,11 @@ extern "C" int hs_batch_set_stage(hs_batch* B, unsigned bytes) {
 }
 extern "C" unsigned hs_batch_get_stage(hs_batch* B) { return B ? B->stage : 0u; }
 
-// Autotuner: for cluster sizes 1, 4, 8 and 4 to 32 executors for the heaviest
-// serialised instance, take the smallest v (1, 2, 4, ...) whose gangs fit, time
-// one replay on a copy of the initial storage, and keep the fastest plan.
+// Autotuner: for staging sizes 40 and 56 KB (four or three CTAs per SM),
+// cluster sizes 1, 4, 8 and 8 to 32 executors for the heaviest serialised
+// instance, take the smallest v (1, 2, 4, ...) whose gangs fit, time one replay
+// on a copy of the initial storage and keep the fastest plan; then try
+// exponential-backoff caps of 256 and 32 ns against the default 1024.
 extern "C" int hs_batch_autotune(hs_batch* B, void* stream, int* best_v, float* best_ms) {
   if (!B) return HS_EINVAL;
   std::vector<std::vector<uint32_t>> saved(B->n);
@@ -539,22 +667,58 @@ extern "C" int hs_batch_autotune(hs_batch* B, void* stream, int* best_v, float* 
   for (const auto& c : B->cfg) max_g = std::max(max_g, c.num_tbs);
   float best_t = 1e30f;
   int bcl = 0, bse = 0, bv = 0;
-  for (int cl : {1, 4, 8}) {
-    for (int se : {4, 8, 16, 32}) {
-      int v = 1;
-      while (v <= max_g && hs_batch_plan_ex(B, cl, se, v, nullptr, nullptr) != HS_OK) v *= 2;
-      if (v > max_g) continue;
-      hs_batch_result r;
-      const int s = hs_batch_run(B, stream, &r);
-      for (int i = 0; i < B->n; ++i) hs_batch_set_storage(B, i, saved[i].data());
-      if (s != HS_OK) continue;
-      if (r.elapsed_ms < best_t) { best_t = r.elapsed_ms; bcl = cl; bse = se; bv = v; }
+  unsigned bstage = B->stage, bbo = B->bo_max;
+  auto trial = [&]() -> float {
+    hs_batch_result r;
+    const int s = hs_batch_run(B, stream, &r);
+    for (int i = 0; i < B->n; ++i) hs_batch_set_storage(B, i, saved[i].data());
+    return s == HS_OK ? r.elapsed_ms : 1e30f;
+  };
+  // staging size (four or three CTAs per SM), cluster size, executors of the
+  // heaviest serialised instance; smallest v that fits
+  for (unsigned stage : {40u * 1024u, 56u * 1024u}) {
+    if (hs_batch_set_stage(B, stage) != HS_OK) continue;
+    for (int cl : {1, 4, 8}) {
+      for (int se : {8, 16, 32}) {
+        int v = 1;
+        while (v <= max_g && hs_batch_plan_ex(B, cl, se, v, nullptr, nullptr) != HS_OK) v *= 2;
+        if (v > max_g) continue;
+        const float t = trial();
+        if (t < best_t) { best_t = t; bcl = cl; bse = se; bv = v; bstage = stage; }
+      }
     }
   }
   if (!bcl) { g_berr = "no plan fits"; return HS_ENORES; }
+  // exponential-backoff cap for the winner
+  hs_batch_set_stage(B, bstage);
+  for (unsigned bo : {256u, 32u}) {
+    hs_batch_set_backoff(B, 1u, bo);
+    if (hs_batch_plan_ex(B, bcl, bse, bv, nullptr, nullptr) != HS_OK) continue;
+    const float t = trial();
+    if (t < best_t) { best_t = t; bbo = bo; }
+  }
+  hs_batch_set_backoff(B, 1u, bbo);
   hs_batch_plan_ex(B, bcl, bse, bv, nullptr, nullptr);
   if (best_v) *best_v = bv;
   if (best_ms) *best_ms = best_t;
+  return HS_OK;
+}
+
+// Exponential-backoff bounds of the batched launch (EBO mutexes and
+// semaphores; bo_max a power of two).  Invalidates the plan.
+extern "C" int hs_batch_set_backoff(hs_batch* B, unsigned bo_min, unsigned bo_max) {
+  if (!B || bo_min == 0 || bo_max < 2 || (bo_max & (bo_max - 1))) return HS_EINVAL;
+  B->bo_min = bo_min;
+  B->bo_max = bo_max;
+  B->grid = 0;
+  if (B->exec) { cudaGraphExecDestroy(B->exec); B->exec = nullptr; }
+  if (B->graph) { cudaGraphDestroy(B->graph); B->graph = nullptr; }
+  return HS_OK;
+}
+extern "C" int hs_batch_get_backoff(hs_batch* B, unsigned* bo_min, unsigned* bo_max) {
+  if (!B) return HS_EINVAL;
+  if (bo_min) *bo_min = B->bo_min;
+  if (bo_max) *bo_max = B->bo_max;
   return HS_OK;
 }
 

@@ -85,8 +85,9 @@ __device__ __forceinline__ void cs_slice(unsigned* data, int s, int L) {
 
 // Semaphore reader: load lines 0..L-1 of the chunk (main.cu:89-100); the loaded
 // values are folded into one word per TB so the loads are not dead.
-__device__ __forceinline__ void cs_read(const unsigned* chunk, int T, int L, unsigned* sink_slot) {
-  const int R = T >> 4;
+// Reader over R consecutive half-warp regions starting at `chunk` (a whole
+// chunk: R = T / 16).
+__device__ __forceinline__ void cs_read_regions(const unsigned* chunk, int R, int T, int L, unsigned* sink_slot) {
   const int rw4 = (L + 1) * 4;
   const int per_region = L * 4;
   const int nitems = R * per_region;
@@ -111,6 +112,10 @@ __device__ __forceinline__ void cs_read(const unsigned* chunk, int T, int L, uns
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
   if ((threadIdx.x & 31) == 0 && acc == 0x9E3779B9u) *sink_slot = acc;  // practically never taken
+}
+
+__device__ __forceinline__ void cs_read(const unsigned* chunk, int T, int L, unsigned* sink_slot) {
+  cs_read_regions(chunk, T >> 4, T, L, sink_slot);
 }
 
 // ---------------------------------------------------------------------------
@@ -281,6 +286,80 @@ __device__ __forceinline__ bool cs_chunk_tma_tiled(const RunDesc& d, int chunk, 
   }
   if (is_master()) {
     asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");  // writes complete before the release
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+  }
+  return true;
+}
+
+// Several chunks' critical sections through one staging buffer: the k chunks
+// (first + i*add) mod mod, regions [r_lo, r_hi) of each, are packed into
+// tiles of whole regions; a tile issues one bulk load per contiguous run (all
+// completing on the one mbarrier), then one bulk store per region.  A
+// semaphore writer's numTBs_perSM chunks thus share tiles instead of paying a
+// load-store round trip each.
+template <int MODE>
+__device__ __forceinline__ bool cs_chunks_tma_tiled(const RunDesc& d, int first, int k, int add, int mod, TmaCtx& t,
+                                                    unsigned buf_bytes, const HsEnv& env, int r_lo, int r_hi) {
+  const int nr = r_hi - r_lo;
+  if (nr <= 0 || k <= 0) return true;
+  const unsigned rb = (unsigned)(64 * (d.L + 1));
+  const size_t cw = chunk_words(d.T, d.L);
+  int per = (int)(buf_bytes / rb);
+  if (per < 1) per = 1;
+  const unsigned sbase = smem_addr(t.buf);
+  const int total = k * nr;
+  auto region_ptr = [&](int p) {
+    const int i = p / nr, r = r_lo + p % nr;
+    const int c = (int)(((long long)first + (long long)i * add) % mod);
+    return reinterpret_cast<unsigned char*>(d.data + (size_t)c * cw) + (size_t)r * rb;
+  };
+  for (int p0 = 0; p0 < total; p0 += per) {
+    const int n = (total - p0 < per) ? (total - p0) : per;
+    if (is_master()) {
+      asm volatile("fence.proxy.async.global;" ::: "memory");
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(t.mbar), "r"((unsigned)n * rb)
+                   : "memory");
+      int q = 0;
+      while (q < n) {  // one bulk load per run of regions contiguous in memory
+        int e = q + 1;
+        while (e < n && (p0 + e) % nr != 0) ++e;
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     :: "r"(sbase + (unsigned)q * rb), "l"(region_ptr(p0 + q)), "r"((unsigned)(e - q) * rb),
+                        "r"(t.mbar)
+                     : "memory");
+        q = e;
+      }
+    }
+    const bool ok = is_master() ? tma_wait(t, env) : true;
+    t.phase ^= 1u;
+    if (__syncthreads_and(ok) == 0) return false;
+    unsigned first_line = 0u;
+    if constexpr (MODE == M_INC) {
+      const int per_region = d.L * 4, rw4 = (d.L + 1) * 4;
+      uint4* s4 = reinterpret_cast<uint4*>(t.buf);
+      for (int i = threadIdx.x; i < n * per_region; i += d.T) {
+        const int h = i / per_region;
+        uint4& v = s4[h * rw4 + 4 + (i - h * per_region)];
+        v.x += 1u; v.y += 1u; v.z += 1u; v.w += 1u;
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+      first_line = 1u;
+    }
+    if (is_master()) {
+      for (int h = 0; h < n; ++h) {
+        asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                     :: "l"(region_ptr(p0 + h) + 64u), "r"(sbase + h * rb + first_line * 64u),
+                        "r"((unsigned)(64 * d.L))
+                     : "memory");
+      }
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+      asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+    }
+    __syncthreads();
+  }
+  if (is_master()) {
+    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
     asm volatile("fence.proxy.async.global;" ::: "memory");
   }
   return true;

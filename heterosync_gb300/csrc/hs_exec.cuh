@@ -115,15 +115,24 @@ __device__ __noinline__ bool cl_sem_op(const RunDesc& d, int b, int cr, int cl, 
   if (!cl_grant(s_ok, ok, cr, cl)) return false;
   bool cs_ok = true;
   if (writer) {
-    int cur = uniq ? b : 0;
-    for (int j = 0; j < k && cs_ok; ++j) {
-      cs_ok = cl_cs<MODE>(d, cur, cr, cl, t, env);
-      cur = uniq ? (cur + numSM) % Gd : cur + 1;
+    if (cl == 1 && d.L <= 16) {
+      int cur = uniq ? b : 0;
+      for (int j = 0; j < k && cs_ok; ++j) {
+        cs_chunk<MODE, 4>(d, cur);
+        cur = uniq ? (cur + numSM) % Gd : cur + 1;
+      }
+    } else {  // the k chunks' shares packed into shared tiles
+      const int R = d.T >> 4, lo = cr * R / cl, hi = (cr + 1) * R / cl;
+      cs_ok = cs_chunks_tma_tiled<MODE>(d, uniq ? b : 0, k, uniq ? numSM : 1, uniq ? Gd : (k > 0 ? k : 1), t, t.cap,
+                                        env, lo, hi);
     }
   } else {
     const int R = d.T >> 4, lo = cr * R / cl, hi = (cr + 1) * R / cl;
     const int rc = uniq ? b : p;
-    if (cl == 1 && d.L <= 16) cs_read(d.data + (size_t)rc * chunk_words(d.T, d.L), d.T, d.L, d.sink + b);
+    const unsigned* c = d.data + (size_t)rc * chunk_words(d.T, d.L);
+    if (cl == 1 && d.L <= 16) cs_read(c, d.T, d.L, d.sink + b);
+    else if (cl > 1 && lo < hi)  // a cluster rank's slice is small: vector loads beat a bulk-copy round trip
+      cs_read_regions(c + (size_t)lo * 16 * (d.L + 1), hi - lo, d.T, d.L, d.sink + b);
     else if (lo < hi) cs_ok = cs_read_tma_tiled(d, rc, t, t.cap, env, d.sink + b, lo, hi);
   }
   cs_ok = cl_end(s_ok, cs_ok, cr, cl);
@@ -165,6 +174,122 @@ __device__ __noinline__ void batch_barrier(const RunDesc& d, int rank, int c, un
       if (!gang_barrier(d, (unsigned)c, gen, env)) return;
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Relaxed-atomics instances (the batch's four extra kinds).  One operation of
+// logical TB b at iteration j; no operation waits on a logical TB that is not
+// running (the seqlock writer waits only for a writer that holds the lock), so
+// any executor count is deadlock-free.  Storage layouts and final states:
+//   RefCounter   : ref[L], total[L]; every thread t takes and drops a reference
+//                  on ref[(b+j+t) % L] (relaxed +1, release -1) and counts it in
+//                  total: ref unchanged, total += number of (b, j, t) per slot
+//                  (refCounter_kernel.cu:4-55 at instance scale).
+//   SplitCounter : one 64-bit partial per logical SM; every warp adds 32*L to
+//                  partial[b % NUM_SM] and the CTA then reads all partials
+//                  (splitCounter_kernel.cu:10-103 with per-SM 64-bit partials).
+//   Seqlock      : 4 x 64-bit payload + torn-read count; the sequence word is
+//                  lock state.  TBs b % 4 == 0 write (CAS even -> odd, payload,
+//                  release +1), the others read with the seqlock retry rule and
+//                  count payloads that do not match their sequence number
+//                  (seqlocks_kernel.cu:17-232 with a 4 x u64 payload).
+//   Flags        : data[L] + violation count; the flag word is lock state.  TB 0
+//                  writes data = j+1 then releases flag = j+1; the others acquire
+//                  the flag and count data words below it (flags_kernel.cu
+//                  stop/dirty message passing, without waiting).
+// ---------------------------------------------------------------------------
+enum : int { P_REFCOUNT = 40, P_SPLITCOUNT = 41, P_SEQLOCK = 42, P_FLAGS = 43 };
+__device__ __forceinline__ bool is_relaxed_prim(int p) { return p >= P_REFCOUNT && p <= P_FLAGS; }
+
+__device__ __forceinline__ unsigned long long seq_pattern(unsigned seq, int i) {
+  return (unsigned long long)seq * 0x9E3779B97F4A7C15ull + (unsigned long long)i;
+}
+
+static __device__ __noinline__ bool relaxed_op(const RunDesc& d, int b, int j, const HsEnv& env) {
+  __shared__ unsigned s_v;
+  const int t = threadIdx.x, T = d.T;
+  unsigned* st = d.data;
+  if (d.prim == P_REFCOUNT) {
+    const int L = d.L;
+    if (t < T) {
+      const int k = (b + j + t) % L;
+      asm volatile("red.relaxed.gpu.global.add.u32 [%0], 1;" :: "l"(st + k) : "memory");
+      asm volatile("red.relaxed.gpu.global.add.u32 [%0], 1;" :: "l"(st + L + k) : "memory");
+      asm volatile("red.release.gpu.global.add.u32 [%0], %1;" :: "l"(st + k), "r"(0xFFFFFFFFu) : "memory");
+    }
+    return true;
+  }
+  if (d.prim == P_SPLITCOUNT) {
+    unsigned long long* part = reinterpret_cast<unsigned long long*>(st);
+    if ((t & 31) == 0 && t < T) {
+      asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;"
+                   :: "l"(part + (b % d.nsm)), "l"((unsigned long long)32 * (unsigned long long)d.L) : "memory");
+    }
+    unsigned long long sum = 0;
+    for (int s2 = t; s2 < d.nsm; s2 += blockDim.x) {
+      unsigned long long v;
+      asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(part + s2) : "memory");
+      sum += v;
+    }
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if ((t & 31) == 0 && sum) atomicAdd(d.sink + b, (unsigned)(sum & 0xFFFFFFFFu));
+    return true;
+  }
+  unsigned* lockw = d.locks + (size_t)d.l_grp * kLineWords;
+  if (d.prim == P_SEQLOCK) {
+    unsigned long long* pay = reinterpret_cast<unsigned long long*>(st);
+    unsigned* torn = st + 8;
+    int ok = 1;
+    if (is_master()) {
+      if (b % 4 == 0) {
+        unsigned cur = 0;
+        ok = wait_until_p([&] {
+               cur = ld_relaxed<GPU>(lockw);
+               return (cur & 1u) == 0u && atom_cas_acquire<GPU>(lockw, cur, cur + 1u) == cur;
+             }, [&] { return ld_relaxed<GPU>(lockw); }, [] {}, env, HS_SITE_RELAXED);
+        if (ok) {
+          asm volatile("fence.acq_rel.gpu;" ::: "memory");  // payload stores stay after the odd sequence number
+          const unsigned v = cur + 2u;
+          for (int i = 0; i < 4; ++i)
+            asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" :: "l"(pay + i), "l"(seq_pattern(v, i)) : "memory");
+          st_release<GPU>(lockw, v);
+        }
+      } else {
+        for (int tries = 0; tries < 64; ++tries) {
+          const unsigned s1 = ld_acquire<GPU>(lockw);
+          if (s1 & 1u) continue;
+          unsigned long long p[4];
+          for (int i = 0; i < 4; ++i)
+            asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(p[i]) : "l"(pay + i) : "memory");
+          asm volatile("fence.acq_rel.gpu;" ::: "memory");
+          if (ld_relaxed<GPU>(lockw) != s1) continue;
+          bool good = true;
+          if (s1 != 0u)
+            for (int i = 0; i < 4; ++i) good = good && p[i] == seq_pattern(s1, i);
+          if (!good) atomicAdd(torn, 1u);
+          break;
+        }
+      }
+    }
+    return __syncthreads_or(!ok) == 0;
+  }
+  // P_FLAGS
+  const int L = d.L;
+  unsigned* data = st;
+  unsigned* viol = st + L;
+  if (b == 0) {
+    for (int k = t; k < L; k += blockDim.x) st_relaxed<GPU>(data + k, (unsigned)j + 1u);
+    __syncthreads();
+    if (is_master()) st_release<GPU>(lockw, (unsigned)j + 1u);
+  } else {
+    if (is_master()) s_v = ld_acquire<GPU>(lockw);
+    __syncthreads();
+    const unsigned f = s_v;
+    for (int k = t; k < L; k += blockDim.x)
+      if (ld_relaxed<GPU>(data + k) < f) atomicAdd(viol, 1u);
+    __syncthreads();
+  }
+  return true;
 }
 
 }  // namespace hs

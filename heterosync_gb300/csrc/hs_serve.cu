@@ -406,7 +406,11 @@ __global__ void __launch_bounds__(kServeThreads, 4) k_serve(ServeArgs a) {
       if (!sbar()) break;
       t_start = globaltimer();
       const HsEnv env{d.status, d.timeout_ns};
-      if (is_mutex_prim(d.prim) || is_sem_prim(d.prim)) {
+      if (is_relaxed_prim(d.prim)) {
+        bool ok = true;
+        for (int j = 0; j < d.iters && ok; ++j)
+          for (int b = rank; b < d.num_tbs && ok; b += a.gang) ok = relaxed_op(d, b, j, env);
+      } else if (is_mutex_prim(d.prim) || is_sem_prim(d.prim)) {
         const bool mtx = is_mutex_prim(d.prim);
         const bool whole = CL && d.prim >= 4 && d.prim <= 15 && d.L >= 33;
         const int ecl = whole ? a.gang : 1, er = whole ? rank : 0;
@@ -647,16 +651,8 @@ extern "C" int hs_serve_start(int slots, int gang, unsigned long long arena_byte
 // Storage words of a request (input = output = the instance's shared data).
 extern "C" int hs_serve_request_words(const hs_serve_request* r, int nsm, size_t* words) {
   if (!r || !words || r->kind != HS_REQ_SYNCPRIM) return HS_EINVAL;
-  hs_run_config c;
-  hs_run_config_default(&c);
-  c.prim = r->prim;
-  c.num_ldst = r->num_ldst;
-  c.num_tbs = r->num_tbs;
-  c.num_iters = r->num_iters;
-  c.threads = 256;
-  c.repeats = 1;
-  c.mode = HS_MODE_INC;
-  return hs_storage_words(&c, nsm, words);
+  const hs_batch_instance x{r->prim, r->num_ldst, r->num_tbs, r->num_iters};
+  return hs_batch_instance_words(&x, nsm, words);
 }
 
 extern "C" int hs_serve_submit(hs_server* S, const hs_serve_request* r, const uint32_t* input, uint32_t* output,
@@ -675,13 +671,26 @@ extern "C" int hs_serve_submit(hs_server* S, const hs_serve_request* r, const ui
   c.repeats = 1;
   c.mode = HS_MODE_INC;
   size_t words = 0;
-  int s = hs_storage_words(&c, S->nsm, &words);
-  if (s) {
-    g_serr = hs_last_error();
-    return s;
-  }
   Layout L;
-  hs_layout_for(&c, S->nsm, &L);
+  const bool relaxed = r->prim >= HS_BATCH_REFCOUNTER && r->prim <= HS_BATCH_FLAGS;
+  if (relaxed) {  // counters / payload / data words; line 4 holds the sequence or flag word
+    const hs_batch_instance x{r->prim, r->num_ldst, r->num_tbs, r->num_iters};
+    if (hs_batch_instance_words(&x, S->nsm, &words) != HS_OK) {
+      g_serr = "bad relaxed-atomics request";
+      return HS_EINVAL;
+    }
+    std::memset(&L, 0, sizeof(L));
+    L.l_grp = 4;
+    L.groups = 1;
+    L.lines = 8;
+  } else {
+    int s = hs_storage_words(&c, S->nsm, &words);
+    if (s) {
+      g_serr = hs_last_error();
+      return s;
+    }
+    hs_layout_for(&c, S->nsm, &L);
+  }
   // pages: status (64 words) | lock lines | ring | sink | data
   const size_t locks = 64, ring = locks + r64((size_t)L.lines * kLineWords), sink = ring + r64(L.ring_words);
   const size_t state_words = sink + r64((size_t)c.num_tbs);
@@ -719,7 +728,7 @@ extern "C" int hs_serve_submit(hs_server* S, const hs_serve_request* r, const ui
   d.num_tbs = c.num_tbs;
   d.iters = c.num_iters;
   d.nsm = S->nsm;
-  d.sem_max = (unsigned)hs_prim_sem_count(c.prim) + 1u;
+  d.sem_max = relaxed ? 1u : (unsigned)hs_prim_sem_count(c.prim) + 1u;
   d.bo_min = 1;
   d.bo_max = 1024;
   d.bo_unit = 0;

@@ -2,7 +2,7 @@
 Poisson arrivals.
 
 The request mix is the mixed-instance generator's (primitive uniform over the
-28 SyncPrims, numTBs log-uniform in [4, 512], numLdSt in [1, 128],
+28 SyncPrims and the four relaxed-atomics kinds, numTBs log-uniform in [4, 512], numLdSt in [1, 128],
 numCSIters in [10, 5000] divided by `iter_div`).  The peak request rate is
 measured first by publishing every request at once; each offered load is then
 a Poisson arrival process at that fraction of the peak over the same requests.
@@ -14,23 +14,22 @@ from __future__ import annotations
 
 import numpy as np
 
-from . import Batch, RunConfig, Server, batch_generate, device_info, expected_storage
+from . import Batch, Server, batch_expected, batch_generate, batch_instance_words, device_info
 
 
 def make_requests(seed: int, n: int, iter_div: int):
     insts = batch_generate(seed=seed, n=n, iter_div=iter_div)
     nsm = device_info()["nsm"]
     rng = np.random.default_rng(seed)
-    inits = [rng.integers(0, 1000, size=Server.request_words(*x, nsm=nsm)).astype(np.uint32) for x in insts]
+    inits = [rng.integers(0, 1000, size=batch_instance_words(x, nsm)).astype(np.uint32) for x in insts]
     return insts, inits
 
 
 def _check(insts, inits, outs, comps):
-    for k, (p, L, G, I) in enumerate(insts):
+    for k, x in enumerate(insts):
         if comps[k]["status"] != 0:
             return False
-        cfg = RunConfig(prim=p, num_ldst=L, num_tbs=G, num_iters=I, threads=256, repeats=1, mode="inc")
-        if not np.array_equal(outs[k], expected_storage(cfg, inits[k])):
+        if not np.array_equal(outs[k], batch_expected(x, inits[k])):
             return False
     return True
 
@@ -72,12 +71,11 @@ def served_sweep(seed: int = 20260101, n: int = 256, iter_div: int = 50, slots: 
         for i, a in enumerate(inits):
             b.set_storage(i, a)
         r = b.run()
-        for i, (p, L, G, I) in enumerate(insts):
-            cfg = RunConfig(prim=p, num_ldst=L, num_tbs=G, num_iters=I, threads=256, repeats=1, mode="inc")
-            exact &= bool(np.array_equal(b.get_storage(i), expected_storage(cfg, inits[i])))
+        for i, x in enumerate(insts):
+            exact &= bool(np.array_equal(b.get_storage(i), batch_expected(x, inits[i])))
         res["offline_batch"] = {"requests_per_s": n / (r.elapsed_ms * 1e-3),
                                 "sync_ops_per_s": ops / (r.elapsed_ms * 1e-3), "ms": r.elapsed_ms,
-                                "plan": list(b.get_plan())}
+                                "plan": list(b.tuned_settings())}
         b.close()
     res["bit_exact"] = bool(exact)
     return res

@@ -141,6 +141,15 @@ const char* hs_noalloc_last_error(void);
  * Instance i runs numTBs logical TBs on a gang of ceil(numTBs / v) co-resident
  * CTAs; every instance has its own storage and lock state; 256 threads per TB. */
 typedef struct hs_batch_instance { int prim, num_ldst, num_tbs, num_iters; } hs_batch_instance;
+/* Batch-only instance kinds beside the 28 SyncPrims ids: the relaxed-atomics
+ * microbenchmarks at instance scale (refCounter_kernel.cu, splitCounter_kernel.cu,
+ * seqlocks_kernel.cu, flags_kernel.cu); 256 threads per TB, numLdSt sets the
+ * counter / data width. */
+enum { HS_BATCH_REFCOUNTER = 40, HS_BATCH_SPLITCOUNTER = 41, HS_BATCH_SEQLOCK = 42, HS_BATCH_FLAGS = 43 };
+int hs_batch_instance_words(const hs_batch_instance* inst, int nsm, size_t* words);
+/* Closed-form final storage of one instance after one run (mode: HS_MODE_INC or HS_MODE_REF). */
+int hs_batch_expected_storage(const hs_batch_instance* inst, int nsm, int mode, const uint32_t* init,
+                              uint32_t* out, size_t words);
 typedef struct hs_batch_result {
   float elapsed_ms;             /* device time of the batch (or of all serial launches) */
   unsigned long long ops;       /* sum of numTBs * numCSIters */
@@ -170,6 +179,10 @@ int hs_batch_plan(hs_batch* b, int v, int* grid, int* capacity);
  * one-CTA executors. */
 int hs_batch_plan_ex(hs_batch* b, int cl, int serial_execs, int v, int* grid, int* capacity);
 int hs_batch_get_plan(hs_batch* b, int* cl, int* serial_execs, int* v, int* grid);
+/* Exponential-backoff bounds (ns; bo_max a power of two) of the batched launch;
+ * the per-launch form keeps the reference's 1..1024.  The autotuner sets them. */
+int hs_batch_set_backoff(hs_batch* b, unsigned bo_min, unsigned bo_max);
+int hs_batch_get_backoff(hs_batch* b, unsigned* bo_min, unsigned* bo_max);
 /* Staging bytes per CTA for bulk-copy critical sections (0 = the largest chunk:
  * whole-chunk copies, fewer CTAs per SM).  Default 40 KiB.  Invalidates the plan. */
 int hs_batch_set_stage(hs_batch* b, unsigned bytes);
@@ -285,7 +298,7 @@ int hs_exchange_run(const uint32_t* host_in, uint32_t* host_out, int n, int elem
 enum { HS_REQ_SYNCPRIM = 0 };
 typedef struct hs_serve_request {
   int kind;                                  /* HS_REQ_SYNCPRIM */
-  int prim, num_ldst, num_tbs, num_iters;    /* the instance */
+  int prim, num_ldst, num_tbs, num_iters;    /* the instance: a SyncPrims id or an HS_BATCH_* kind */
 } hs_serve_request;
 typedef struct hs_serve_completion {
   unsigned long long id;

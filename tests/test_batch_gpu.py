@@ -8,9 +8,7 @@ pytestmark = pytest.mark.gpu
 
 
 def _expected(hs, inst, init, mode):
-    prim, L, G, I = inst
-    cfg = hs.RunConfig(prim=prim, num_ldst=L, num_tbs=G, num_iters=I, threads=256, repeats=1, mode=mode)
-    return hs.expected_storage(cfg, init)
+    return hs.batch_expected(inst, init, mode=mode)
 
 
 def _run_both(hs, insts, mode="inc"):
@@ -35,7 +33,8 @@ def _run_both(hs, insts, mode="inc"):
 
 def test_every_primitive_once(hs):
     insts = [(p, 7 + (p % 5) * 9, 3 + p % 13, 6 + p % 4) for p in
-             [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30, 31]]
+             [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30, 31,
+              40, 41, 42, 43]]
     rs, rb, v = _run_both(hs, insts)
     assert rb.grid > 0 and rb.ops == rs.ops
     assert rs.launches >= len(insts)
@@ -85,3 +84,14 @@ def test_cluster_plans_bit_exact(hs, cl, mode):
         for i, a in enumerate(inits):
             assert np.array_equal(b.get_storage(i), _expected(hs, insts[i], a, mode)), (cl, se, i, insts[i])
     b.close()
+
+
+
+@pytest.mark.parametrize("kind", [40, 41, 42, 43])
+def test_relaxed_kinds(hs, kind):
+    """RefCounter, SplitCounter, Seqlock (4 x u64 payload) and Flags instances:
+    final counters, payload and data exact, no torn seqlock read and no flag
+    violation (those counts are part of the compared storage), batched and
+    per-launch."""
+    insts = [(kind, L, G, I) for (L, G, I) in [(1, 4, 50), (17, 64, 20), (128, 300, 8), (64, 512, 3)]]
+    _run_both(hs, insts)

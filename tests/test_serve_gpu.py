@@ -13,9 +13,7 @@ PRIMS = [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 20, 21, 22, 23, 2
 
 
 def _expected(hs, inst, init):
-    p, L, G, I = inst
-    cfg = hs.RunConfig(prim=p, num_ldst=L, num_tbs=G, num_iters=I, threads=256, repeats=1, mode="inc")
-    return hs.expected_storage(cfg, init)
+    return hs.batch_expected(inst, init)
 
 
 def _requests(hs, seed):
@@ -23,7 +21,7 @@ def _requests(hs, seed):
     insts += hs.batch_generate(seed=seed, n=16, iter_div=400)
     rng = np.random.default_rng(seed)
     nsm = hs.device_info()["nsm"]
-    inits = [rng.integers(0, 2 ** 32, size=hs.Server.request_words(*x, nsm=nsm), dtype=np.uint64).astype(np.uint32)
+    inits = [rng.integers(0, 2 ** 32, size=hs.batch_instance_words(x, nsm), dtype=np.uint64).astype(np.uint32)
              for x in insts]
     return insts, inits
 
