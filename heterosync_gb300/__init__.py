@@ -477,12 +477,45 @@ def exchange_run(buffers, cluster: int, lf: bool, episodes: int, timeout_ns: int
 # ---------------------------------------------------------------------------
 # Served request loop (hs_serve_*)
 # ---------------------------------------------------------------------------
-REQ_SYNCPRIM = 0
+REQ_SYNCPRIM, REQ_UTS_GEO = 0, 1
 
 
 class _ServeRequest(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int), ("prim", ctypes.c_int), ("num_ldst", ctypes.c_int),
-                ("num_tbs", ctypes.c_int), ("num_iters", ctypes.c_int)]
+                ("num_tbs", ctypes.c_int), ("num_iters", ctypes.c_int), ("seed", ctypes.c_uint),
+                ("depth_limit", ctypes.c_int), ("branching", ctypes.c_double)]
+
+
+def _request(inst):
+    """A request from (prim, num_ldst, num_tbs, num_iters) or ("uts", seed, depth_limit, branching)."""
+    if inst[0] == "uts":
+        _, seed, depth, b = inst
+        return _ServeRequest(REQ_UTS_GEO, 0, 0, 0, 0, seed, depth, b)
+    p, L, G, I = inst
+    return _ServeRequest(REQ_SYNCPRIM, prim_id(p) if isinstance(p, str) else p, L, G, I, 0, 0, 0.0)
+
+
+def serve_request_words(inst, nsm: int = 0) -> int:
+    nsm = nsm or device_info()["nsm"]
+    r = _request(inst)
+    w = ctypes.c_size_t()
+    lib().hs_serve_request_words.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    s = lib().hs_serve_request_words(ctypes.byref(r), nsm, ctypes.byref(w))
+    if s:
+        raise HsError(s, "request words")
+    return int(w.value)
+
+
+def serve_uts_counts(final_words):
+    """(nodes, leaves, deepest level) from a tree-search request's final state."""
+    np = _np()
+    a = np.ascontiguousarray(final_words, dtype=np.uint32)
+    n, lv, d = ctypes.c_ulonglong(), ctypes.c_ulonglong(), ctypes.c_uint()
+    lib().hs_serve_uts_geo_counts.argtypes = [ctypes.c_void_p, ctypes.c_size_t] + [ctypes.c_void_p] * 3
+    s = lib().hs_serve_uts_geo_counts(_p(a), a.size, ctypes.byref(n), ctypes.byref(lv), ctypes.byref(d))
+    if s:
+        raise HsError(s, "tree-search counts")
+    return n.value, lv.value, d.value
 
 
 class _ServeCompletion(ctypes.Structure):
@@ -530,26 +563,23 @@ class Server:
 
     @staticmethod
     def request_words(prim, num_ldst, num_tbs, num_iters, nsm: int = 0):
-        nsm = nsm or device_info()["nsm"]
-        r = _ServeRequest(REQ_SYNCPRIM, prim_id(prim) if isinstance(prim, str) else prim, num_ldst, num_tbs,
-                          num_iters)
-        w = ctypes.c_size_t()
-        lib().hs_serve_request_words.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
-        s = lib().hs_serve_request_words(ctypes.byref(r), nsm, ctypes.byref(w))
-        if s:
-            raise HsError(s, "request words")
-        return int(w.value)
+        return serve_request_words((prim, num_ldst, num_tbs, num_iters), nsm)
 
-    def submit(self, inst, init):
-        """inst = (prim, num_ldst, num_tbs, num_iters); init = the initial
-        storage (uint32).  Returns (id, output array filled at completion)."""
+    def submit(self, inst, init=None):
+        """inst = (prim, num_ldst, num_tbs, num_iters) with init = the initial
+        storage (uint32), or ("uts", seed, depth_limit, branching) with no
+        init.  Returns (id, output array filled at completion)."""
         np = _np()
-        prim, L, G, I = inst
-        r = _ServeRequest(REQ_SYNCPRIM, prim_id(prim) if isinstance(prim, str) else prim, L, G, I)
-        init = np.ascontiguousarray(init, dtype=np.uint32)
-        out = np.zeros_like(init)
+        r = _request(inst)
+        if inst[0] == "uts":
+            out = np.zeros(serve_request_words(inst), dtype=np.uint32)
+            init_p = None
+        else:
+            init = np.ascontiguousarray(init, dtype=np.uint32)
+            out = np.zeros_like(init)
+            init_p = _p(init)
         rid = ctypes.c_ulonglong()
-        self._check(lib().hs_serve_submit(self.h, ctypes.byref(r), _p(init), _p(out), ctypes.byref(rid)))
+        self._check(lib().hs_serve_submit(self.h, ctypes.byref(r), init_p, _p(out), ctypes.byref(rid)))
         self._keep[rid.value] = out
         return rid.value, out
 
@@ -579,11 +609,11 @@ class Server:
         (outputs, completions in request order, wall seconds)."""
         np = _np()
         n = len(insts)
-        reqs = (_ServeRequest * n)(*[_ServeRequest(REQ_SYNCPRIM, p if not isinstance(p, str) else prim_id(p), L, G, I)
-                                     for (p, L, G, I) in insts])
-        ins = [np.ascontiguousarray(x, dtype=np.uint32) for x in inits]
-        outs = [np.zeros_like(x) for x in ins]
-        in_p = (ctypes.c_void_p * n)(*[x.ctypes.data for x in ins])
+        reqs = (_ServeRequest * n)(*[_request(x) for x in insts])
+        ins = [None if x[0] == "uts" else np.ascontiguousarray(a, dtype=np.uint32) for x, a in zip(insts, inits)]
+        outs = [np.zeros(serve_request_words(x), dtype=np.uint32) if x[0] == "uts" else np.zeros_like(a)
+                for x, a in zip(insts, ins)]
+        in_p = (ctypes.c_void_p * n)(*[None if a is None else a.ctypes.data for a in ins])
         out_p = (ctypes.c_void_p * n)(*[x.ctypes.data for x in outs])
         arr = np.ascontiguousarray(arrival_s, dtype=np.float64)
         comps = (_ServeCompletion * n)()

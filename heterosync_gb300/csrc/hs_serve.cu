@@ -39,6 +39,7 @@
 #include <unordered_map>
 #include <vector>
 #include "hs_exec.cuh"
+#include "hs_uts_geo.cuh"
 #include "../../include/hs/hs.h"
 
 void hs_note_launches(unsigned n);
@@ -95,6 +96,35 @@ struct ServeCtl {  // device memory
 };
 
 enum : int { CMD_IDLE = 0, CMD_RUN = 1, CMD_STOP = 2, CMD_REJECT = 3, CMD_WAIT = 4 };
+
+// Tree-search requests: the walk's state image (copied in and out as the
+// request's storage) and its queue items (lock-state pages, zeroed).
+//   word 0 work, 32 idle, 64.. counts (u64 at byte offsets 0, 64, 128),
+//   160 seed, 161 depth limit, 162 table length, 163 queues,
+//   192 thresholds (128), 320 queue positions (64 per queue), then the
+//   queues' cell sequence numbers (kGeoQueueCap per queue).
+constexpr int kPrimUtsGeo = 50;
+constexpr int kUtsQueues = 8;
+constexpr size_t kUtsImageWords = 320 + (size_t)kUtsQueues * 64 + (size_t)kUtsQueues * kGeoQueueCap;
+
+__device__ __forceinline__ void serve_uts_geo(const RunDesc& d, unsigned rank) {
+  unsigned* base = d.data;
+  GeoArgs g;
+  g.work = base;
+  g.idle = base + 32;
+  g.out = reinterpret_cast<unsigned long long*>(base + 64);
+  g.seed = base[160];
+  g.limit = (int)base[161];
+  g.nt = (int)base[162];
+  g.nq = (int)base[163];
+  g.table = base + 192;
+  g.qpos = base + 320;
+  g.qseq = base + 320 + (size_t)g.nq * 64;
+  g.qitem = reinterpret_cast<GeoItem*>(d.ring);
+  g.status = d.status;
+  g.timeout_ns = d.timeout_ns;
+  uts_geo_walk(g, rank);
+}
 
 struct __align__(128) SlotBox {  // per slot; written by its rank-0 CTA before a slot barrier
   RunDesc d;                     // absolute pointers
@@ -406,7 +436,9 @@ __global__ void __launch_bounds__(kServeThreads, 4) k_serve(ServeArgs a) {
       if (!sbar()) break;
       t_start = globaltimer();
       const HsEnv env{d.status, d.timeout_ns};
-      if (is_relaxed_prim(d.prim)) {
+      if (d.prim == kPrimUtsGeo) {
+        serve_uts_geo(d, (unsigned)rank);
+      } else if (is_relaxed_prim(d.prim)) {
         bool ok = true;
         for (int j = 0; j < d.iters && ok; ++j)
           for (int b = rank; b < d.num_tbs && ok; b += a.gang) ok = relaxed_op(d, b, j, env);
@@ -650,15 +682,32 @@ extern "C" int hs_serve_start(int slots, int gang, unsigned long long arena_byte
 
 // Storage words of a request (input = output = the instance's shared data).
 extern "C" int hs_serve_request_words(const hs_serve_request* r, int nsm, size_t* words) {
+  if (r && words && r->kind == HS_REQ_UTS_GEO) {
+    *words = kUtsImageWords;
+    return HS_OK;
+  }
   if (!r || !words || r->kind != HS_REQ_SYNCPRIM) return HS_EINVAL;
   const hs_batch_instance x{r->prim, r->num_ldst, r->num_tbs, r->num_iters};
   return hs_batch_instance_words(&x, nsm, words);
 }
 
+extern "C" int hs_serve_uts_geo_counts(const uint32_t* w, size_t words, unsigned long long* nodes,
+                                       unsigned long long* leaves, unsigned* deepest) {
+  if (!w || words < kUtsImageWords) return HS_EINVAL;
+  auto u64 = [&](size_t at) { return (unsigned long long)w[at] | ((unsigned long long)w[at + 1] << 32); };
+  if (nodes) *nodes = u64(64);
+  if (leaves) *leaves = u64(80);
+  if (deepest) *deepest = (unsigned)u64(96);
+  return HS_OK;
+}
+
+static int submit_uts_geo(hs_server* S, const hs_serve_request* r, uint32_t* output, unsigned long long* id_out);
+
 extern "C" int hs_serve_submit(hs_server* S, const hs_serve_request* r, const uint32_t* input, uint32_t* output,
                                unsigned long long* id_out) {
+  if (S && r && output && r->kind == HS_REQ_UTS_GEO) return submit_uts_geo(S, r, output, id_out);
   if (!S || !r || !input || !output || r->kind != HS_REQ_SYNCPRIM) {
-    g_serr = "need a server, a SyncPrims request, input and output";
+    g_serr = "need a server, a SyncPrims or tree-search request, input and output";
     return HS_EINVAL;
   }
   hs_run_config c;
@@ -756,6 +805,81 @@ extern "C" int hs_serve_submit(hs_server* S, const hs_serve_request* r, const ui
   __atomic_store_n(&S->hctl->tail, S->submitted, __ATOMIC_RELEASE);
   if (id_out) *id_out = id;
   return HS_OK;
+}
+
+// Publish a ready descriptor whose storage image (words) is `image`.
+static int publish(hs_server* S, ServeDesc& q, const uint32_t* image, size_t words, uint32_t* output, double t_submit,
+                   unsigned long long* id_out) {
+  std::lock_guard<std::mutex> g(S->mu);
+  if (!S->running) {
+    g_serr = "server stopped";
+    return HS_EINVAL;
+  }
+  const unsigned slot = (unsigned)(S->submitted % kServeQ);
+  if (S->submitted - S->polled >= std::min(kServeQ, kServeC) - 1 || S->ring_busy[slot]) {
+    g_serr = "too many requests in flight";
+    return HS_ENORES;
+  }
+  size_t off = 0;
+  if (stage_alloc(S, words * 4, &off) != HS_OK) {
+    g_serr = "staging pool full";
+    return HS_ENORES;
+  }
+  std::memcpy(S->hblock + S->staging_off + off, image, words * 4);
+  const unsigned long long id = S->next_id++;
+  q.id = id;
+  q.stage_off = off;
+  q.words = words;
+  std::memcpy(&S->ring[slot], &q, sizeof(q));
+  S->ring_busy[slot] = 1;
+  S->pending[id] = hs_server::Pending{off, words * 4, output, words, t_submit, slot};
+  S->submitted += 1;
+  std::atomic_thread_fence(std::memory_order_release);
+  __atomic_store_n(&S->hctl->tail, S->submitted, __ATOMIC_RELEASE);
+  if (id_out) *id_out = id;
+  return HS_OK;
+}
+
+static int submit_uts_geo(hs_server* S, const hs_serve_request* r, uint32_t* output, unsigned long long* id_out) {
+  if (r->depth_limit < 0 || r->depth_limit > kGeoMaxDepth || !(r->branching > 0.0)) {
+    g_serr = "tree search needs 0 <= depth_limit <= 30 and branching > 0";
+    return HS_EINVAL;
+  }
+  const double t_submit = now_s();
+  std::vector<uint32_t> img(kUtsImageWords, 0u);
+  img[0] = 1u;  // work: the root's thread
+  img[160] = r->seed;
+  img[161] = (uint32_t)r->depth_limit;
+  img[162] = (uint32_t)hs_uts_geo_table(r->branching, img.data() + 192, kGeoTable);
+  img[163] = (uint32_t)kUtsQueues;
+  for (int qn = 0; qn < kUtsQueues; ++qn)
+    for (unsigned i = 0; i < kGeoQueueCap; ++i) img[320 + kUtsQueues * 64 + qn * kGeoQueueCap + i] = i;
+  // pages: status (64 words) | queue items (lock state, zeroed) | sink | image
+  const size_t items = 64, sink = items + r64((size_t)kUtsQueues * kGeoQueueCap * (sizeof(GeoItem) / 4));
+  const size_t state_words = sink + 64;
+  ServeDesc q;
+  std::memset(&q, 0, sizeof(q));
+  RunDesc& d = q.d;
+  d.status = reinterpret_cast<unsigned*>((size_t)0);
+  d.locks = reinterpret_cast<unsigned*>(items * 4);
+  d.ring = reinterpret_cast<unsigned*>(items * 4);
+  d.sink = reinterpret_cast<unsigned*>(sink * 4);
+  d.data = reinterpret_cast<unsigned*>(state_words * 4);
+  d.prim = kPrimUtsGeo;
+  d.mode = HS_MODE_INC;
+  d.T = 256;
+  d.num_tbs = 1;
+  d.iters = 1;
+  d.nsm = S->nsm;
+  d.sem_max = 1;
+  d.timeout_ns = 10000000000ull;
+  d.skip_tb = -1;
+  d.cluster = 1;
+  q.state_words = state_words;
+  q.pages = ((state_words + r64(kUtsImageWords)) * 4 + kPageBytes - 1) / kPageBytes;
+  q.groups = 0;
+  q.ring_groups = 0;
+  return publish(S, q, img.data(), kUtsImageWords, output, t_submit, id_out);
 }
 
 static int poll_locked(hs_server* S, hs_serve_completion* out, int max, int* n) {

@@ -295,11 +295,19 @@ int hs_exchange_run(const uint32_t* host_in, uint32_t* host_out, int n, int elem
  * Between hs_serve_start and hs_serve_stop the server kernel occupies the
  * device: the process must not make synchronising CUDA calls on it
  * (cudaDeviceSynchronize, cudaMalloc, cudaFree) until the server stopped. */
-enum { HS_REQ_SYNCPRIM = 0 };
+enum { HS_REQ_SYNCPRIM = 0, HS_REQ_UTS_GEO = 1 };
 typedef struct hs_serve_request {
-  int kind;                                  /* HS_REQ_SYNCPRIM */
-  int prim, num_ldst, num_tbs, num_iters;    /* the instance: a SyncPrims id or an HS_BATCH_* kind */
+  int kind;                                  /* HS_REQ_SYNCPRIM or HS_REQ_UTS_GEO */
+  int prim, num_ldst, num_tbs, num_iters;    /* SYNCPRIM: a SyncPrims id or an HS_BATCH_* kind */
+  unsigned seed;                             /* UTS_GEO: the geometric tree (hs_uts_geo_run) */
+  int depth_limit;
+  double branching;
 } hs_serve_request;
+/* A tree-search request's input may be NULL (the server builds the walk's
+ * initial state); its output (hs_serve_request_words words) holds the final
+ * state, from which this reads the counts. */
+int hs_serve_uts_geo_counts(const uint32_t* final_words, size_t words, unsigned long long* nodes,
+                            unsigned long long* leaves, unsigned* deepest);
 typedef struct hs_serve_completion {
   unsigned long long id;
   int status;                 /* HS_OK; HS_ENORES: larger than the arena; HS_ETIMEDOUT: a wait ran out */

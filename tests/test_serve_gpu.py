@@ -124,3 +124,38 @@ def test_stop_drains_then_idle_exit(hs):
         srv.stop(timeout_s=5.0)
     finally:
         srv.close()
+
+
+def test_tree_search_requests_alone_and_in_mix(hs, oracle):
+    """Geometric SHA-1 UTS requests run on a slot's CTAs (work stealing over
+    the slot's queues): counts exact against the oracle, the same alone and
+    mixed with SyncPrims requests."""
+    trees = [("uts", s, d, 4.0) for s, d in [(2, 6), (3, 7), (4, 8), (5, 9), (7, 5), (11, 8)]]
+    insts, inits = _requests(hs, 404)
+    srv = hs.Server(slots=8, gang=8, arena_bytes=512 << 20, staging_bytes=256 << 20, idle_timeout_s=20.0)
+    try:
+        alone = []
+        for t in trees:
+            rid, out = srv.submit(t)
+            c = srv.wait(1)[0]
+            assert c["status"] == 0
+            alone.append(hs.serve_uts_counts(out))
+        mixed = list(zip(trees + insts, [None] * len(trees) + inits))
+        outs = {}
+        for x, a in mixed:
+            rid, out = srv.submit(x, a)
+            outs[rid] = (x, a, out)
+        comps = {c["id"]: c for c in srv.wait(len(mixed))}
+        srv.stop()
+    finally:
+        srv.close()
+    for t, got in zip(trees, alone):
+        assert got == oracle.geo_count(t[1], t[2], t[3]), t
+    k = 0
+    for rid, (x, a, out) in outs.items():
+        assert comps[rid]["status"] == 0
+        if x[0] == "uts":
+            assert hs.serve_uts_counts(out) == alone[k], x
+            k += 1
+        else:
+            assert np.array_equal(out, _expected(hs, x, a)), x
