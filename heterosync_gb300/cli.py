@@ -11,8 +11,12 @@
       each offered load; p50/p99 latency, throughput, the offline batch of the
       same requests, bit-exact check of every result
 
+  python -m heterosync_gb300.cli uts-geo [--seed 2] [--depth 12]
+         [--branching 4] [--blocks 304] [--threads 256]
+      geometric SHA-1 UTS by work stealing; node, leaf and depth counts
+
   python -m heterosync_gb300.cli batch [--seed 20260101] [--n 64]
-         [--iter-div 1] [--tune-div 25]
+         [--iter-div 1] [--tune-div 25] [--plan cl,se,v,stage,bo]
       the mixed-instance batch: one launch per instance, then the autotuned
       persistent graph-replayed launch; prints one JSON line (both times, the
       ratio, the plan, bit-exact check of every instance)
@@ -45,10 +49,13 @@ def cmd_exchange(a):
 
 def cmd_batch(a):
     insts = batch_generate(seed=a.seed, n=a.n, iter_div=a.iter_div)
-    tb = Batch(batch_generate(seed=a.seed, n=a.n, iter_div=a.tune_div), mode="inc")
-    tb.autotune()
-    tuned = tb.tuned_settings()
-    tb.close()
+    if a.plan:
+        tuned = tuple(int(v) for v in a.plan.split(","))
+    else:
+        tb = Batch(batch_generate(seed=a.seed, n=a.n, iter_div=a.tune_div), mode="inc")
+        tb.autotune()
+        tuned = tb.tuned_settings()
+        tb.close()
     b = Batch(insts, mode="inc")
     rng = np.random.default_rng(a.seed)
     inits = [rng.integers(0, 1000, size=b.words(i)).astype(np.uint32) for i in range(len(insts))]
@@ -75,6 +82,15 @@ def cmd_batch(a):
     return 0 if ok_serial and ok_batch else 1
 
 
+def cmd_uts_geo(a):
+    from . import uts_geo_run
+    nodes, leaves, deepest, ms = uts_geo_run(a.seed, a.depth, a.branching, blocks=a.blocks, threads=a.threads)
+    print(json.dumps({"workload": "uts-geo", "seed": a.seed, "depth_limit": a.depth, "branching": a.branching,
+                      "nodes": nodes, "leaves": leaves, "deepest": deepest, "ms": ms,
+                      "nodes_per_s": nodes / (ms * 1e-3) if ms > 0 else None}), flush=True)
+    return 0
+
+
 def cmd_serve(a):
     from .served import served_sweep
     loads = tuple(float(x) / 100.0 for x in a.loads.split(","))
@@ -99,6 +115,13 @@ def main(argv=None):
     bt.add_argument("--n", type=int, default=64)
     bt.add_argument("--iter-div", type=int, default=1)
     bt.add_argument("--tune-div", type=int, default=25)
+    bt.add_argument("--plan", default="", help="cluster,serial_executors,v,stage_bytes,backoff_max_ns: skip tuning")
+    ug = sub.add_parser("uts-geo")
+    ug.add_argument("--seed", type=int, default=2)
+    ug.add_argument("--depth", type=int, default=12)
+    ug.add_argument("--branching", type=float, default=4.0)
+    ug.add_argument("--blocks", type=int, default=304)
+    ug.add_argument("--threads", type=int, default=256)
     sv = sub.add_parser("serve")
     sv.add_argument("--seed", type=int, default=20260101)
     sv.add_argument("--n", type=int, default=256)
@@ -108,7 +131,7 @@ def main(argv=None):
     sv.add_argument("--loads", default="10,30,50,70,90", help="offered loads, percent of the measured peak")
     sv.add_argument("--no-offline", action="store_true")
     a = ap.parse_args(argv)
-    return {"exchange": cmd_exchange, "batch": cmd_batch, "serve": cmd_serve}[a.cmd](a)
+    return {"exchange": cmd_exchange, "batch": cmd_batch, "serve": cmd_serve, "uts-geo": cmd_uts_geo}[a.cmd](a)
 
 
 if __name__ == "__main__":
