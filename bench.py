@@ -339,6 +339,18 @@ def serve_extra(hs):
     return r
 
 
+def combine_ranks(dist, dev_s, e2e_s, ops, device):
+    """Whole-job figures of a replicas run: the slowest rank's device and wall
+    times (max over ranks) and every rank's operations (sum)."""
+    import torch
+    t = torch.tensor([dev_s, e2e_s, float(ops)], device=device, dtype=torch.float64)
+    mx = t.clone()
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    sm = t.clone()
+    dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+    return mx[0].item(), mx[1].item(), int(sm[2].item())
+
+
 def reference_arm(args, rank):
     import oracle
     hs_nsm = None
@@ -470,12 +482,7 @@ def main():
     dev_s = sum(r["ms"] for r in recs) * 1e-3
     e2e_s = sum(r["wall_s"] for r in recs)
     if dist is not None:
-        t = torch.tensor([dev_s, e2e_s, float(ops)], device="cuda", dtype=torch.float64)
-        mx = t.clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        sm = t.clone()
-        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
-        dev_s, e2e_s, ops = mx[0].item(), mx[1].item(), int(sm[2].item())
+        dev_s, e2e_s, ops = combine_ranks(dist, dev_s, e2e_s, ops, "cuda")
 
     if rank == 0:
         peak_gbs, peak_kind = load_peaks()
