@@ -17,7 +17,9 @@ the 6 points, so the default 6 timed steps cover the sweep once.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
-Beside the sweep, outside its timed region, the line carries "exchange" (tree
+Beside the sweep, outside its timed region, the line carries "fa_mutex_slice"
+(faMutex, 8 TBs, numLdSt 10, 100 iterations: the one-launch slice workload),
+"exchange" (tree
 barrier with local exchange on thread-block clusters: 592 CTAs, fp32[4096] per
 CTA rotated every episode, 1000 episodes, cluster sizes 1/2/4/8) and "batch"
 (the 64-instance mixed batch, one launch per instance against the autotuned
@@ -239,6 +241,35 @@ def cs_bytes(name, G, L, nsm):
         readers = G - writers
         return ITERS * (writers * k * T * L * 8 + readers * T * L * 4)
     return G * ITERS * T * L * 8
+
+
+def fa_mutex_slice_extra(hs, nsm):
+    """faMutex (ticket lock), one launch: numTBs 8 x 256 threads, numLdSt 10,
+    numCSIters 100 on uint32[80] seeded in [0, 1000); every critical section
+    adds 1 to a 10-word slice.  Device rate (median of 20 launches), e2e rate
+    through hs_run with host storage, and the host std::thread run of the same
+    algorithm (bit-exact with the GPU's result)."""
+    import oracle
+    cfg = hs.RunConfig(prim="faMutex", num_ldst=10, num_tbs=8, num_iters=100, threads=256, repeats=1, mode="slice")
+    rng = np.random.default_rng(SEED)
+    init = (rng.integers(0, 2 ** 63, size=hs.storage_words(cfg), dtype=np.uint64) % 1000).astype(np.uint32)
+    want = hs.expected_storage(cfg, init)
+    dev, wall = [], []
+    for _ in range(20):
+        st = init.copy()
+        t0 = time.perf_counter()
+        r = hs.run(cfg, st)
+        wall.append(time.perf_counter() - t0)
+        dev.append(r.elapsed_ms * 1e-3)
+        if not np.array_equal(st, want):
+            raise SystemExit("bench: faMutex slice result differs from the expected final state")
+    ops = 8 * 100
+    twin, secs = oracle.twin_run(7, 256, 10, 8, 100, 1, nsm, 2, init)
+    return {"workload": "faMutex slice, numTBs 8 x 256, numLdSt 10, numCSIters 100, one launch",
+            "ops_per_launch": ops, "sync_ops_per_s": ops / statistics.median(dev),
+            "e2e_sync_ops_per_s": ops / statistics.median(wall), "us_per_op": statistics.median(dev) * 1e6 / ops,
+            "cpu_baseline": {"sync_ops_per_s": ops / secs if secs > 0 else None, "kind": "port",
+                             "cores": os.cpu_count(), "bit_exact_with_gpu": bool(np.array_equal(twin, want))}}
 
 
 def exchange_extra(hs):
@@ -540,8 +571,8 @@ def main():
         if ck:
             out["clocks"] = ck
         if not args.no_extras and world == 1:
-            for key, fn in (("exchange", exchange_extra), ("batch", batch_extra), ("serve", serve_extra),
-                            ("uts_geo", uts_geo_extra)):
+            for key, fn in (("fa_mutex_slice", lambda h: fa_mutex_slice_extra(h, nsm)), ("exchange", exchange_extra),
+                            ("batch", batch_extra), ("serve", serve_extra), ("uts_geo", uts_geo_extra)):
                 try:
                     out[key] = fn(hs)
                 except SystemExit:
