@@ -15,6 +15,11 @@
          [--branching 4] [--blocks 304] [--threads 256]
       geometric SHA-1 UTS by work stealing; node, leaf and depth counts
 
+  python -m heterosync_gb300.cli sweep [--prims "..."] [--num-ldst 10]
+         [--num-tbs ...] [--iters 10] [--runs 1]
+      the results-script sweep through the drop-in program; one JSON line per
+      (primitive, numLdSt, numTBs) with the parsed `average` durations
+
   python -m heterosync_gb300.cli batch [--seed 20260101] [--n 64]
          [--iter-div 1] [--tune-div 25] [--plan cl,se,v,stage,bo]
       the mixed-instance batch: one launch per instance, then the autotuned
@@ -91,6 +96,41 @@ def cmd_uts_geo(a):
     return 0
 
 
+SWEEP_PRIMS = ("atomicTreeBarrUniq atomicTreeBarrUniqLocalExch lfTreeBarrUniq lfTreeBarrUniqLocalExch spinMutex "
+               "spinMutexEBO faMutex sleepMutex spinSem10 spinSemEBO10 spinMutexUniq spinMutexEBOUniq faMutexUniq "
+               "sleepMutexUniq spinSemUniq10 spinSemEBOUniq10")
+
+
+def cmd_sweep(a):
+    """The results-script sweep (syncPrims_results.sh:1-59): every primitive x
+    numLdSt x numTBs through the drop-in program, its `average` field parsed as
+    the script parses it (third ':' field, up to 'm'); one JSON line per point."""
+    import os
+    import subprocess
+    from . import device_info
+    exe = os.path.join(os.path.dirname(os.path.abspath(__file__)), "bin", "allSyncPrims-1kernel")
+    nsm = device_info()["nsm"]
+    tbs = [int(x) for x in a.num_tbs.split(",")] if a.num_tbs else [m * nsm for m in (1, 2, 4, 8)]
+    ok = True
+    for prim in a.prims.split():
+        for L in (int(x) for x in a.num_ldst.split(",")):
+            for G in tbs:
+                durations = []
+                for _ in range(a.runs):
+                    p = subprocess.run([exe, prim, str(L), str(G), str(a.iters)], capture_output=True, text=True)
+                    line = next((x for x in p.stdout.splitlines() if "average" in x), "")
+                    try:
+                        durations.append(float(line.split(":")[2].split("m")[0]))
+                    except (IndexError, ValueError):
+                        durations.append(None)
+                    ok = ok and p.returncode == 0 and "PASSED" in p.stdout
+                vals = [d for d in durations if d is not None]
+                print(json.dumps({"syncPrim": prim, "numLdSt": L, "numTBs": G, "numCSIters": a.iters,
+                                  "durations_ms": durations,
+                                  "average_ms": sum(vals) / len(vals) if vals else None}), flush=True)
+    return 0 if ok else 1
+
+
 def cmd_serve(a):
     from .served import served_sweep
     loads = tuple(float(x) / 100.0 for x in a.loads.split(","))
@@ -122,6 +162,12 @@ def main(argv=None):
     ug.add_argument("--branching", type=float, default=4.0)
     ug.add_argument("--blocks", type=int, default=304)
     ug.add_argument("--threads", type=int, default=256)
+    sw = sub.add_parser("sweep")
+    sw.add_argument("--prims", default=SWEEP_PRIMS)
+    sw.add_argument("--num-ldst", default="10")
+    sw.add_argument("--num-tbs", default="", help="comma list; default 1, 2, 4, 8 TBs per SM")
+    sw.add_argument("--iters", type=int, default=10)
+    sw.add_argument("--runs", type=int, default=1)
     sv = sub.add_parser("serve")
     sv.add_argument("--seed", type=int, default=20260101)
     sv.add_argument("--n", type=int, default=256)
@@ -131,7 +177,8 @@ def main(argv=None):
     sv.add_argument("--loads", default="10,30,50,70,90", help="offered loads, percent of the measured peak")
     sv.add_argument("--no-offline", action="store_true")
     a = ap.parse_args(argv)
-    return {"exchange": cmd_exchange, "batch": cmd_batch, "serve": cmd_serve, "uts-geo": cmd_uts_geo}[a.cmd](a)
+    return {"exchange": cmd_exchange, "batch": cmd_batch, "serve": cmd_serve, "uts-geo": cmd_uts_geo,
+            "sweep": cmd_sweep}[a.cmd](a)
 
 
 if __name__ == "__main__":

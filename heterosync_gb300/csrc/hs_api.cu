@@ -457,6 +457,28 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c, void* storage, int on
   // multiple of NUM_SM, 2 to 8 per group) run each group as one thread-block
   // cluster: the local stage becomes the hardware cluster barrier.
   int cluster = 1;
+  // Uniq mutexes and semaphores with whole groups of 2, 4 or 8 TBs per logical
+  // SM run each group as one cluster (lock word in distributed shared memory).
+  if ((is_umutex(c->prim) || is_usem(c->prim)) && !(c->flags & HS_RUN_NO_CLUSTER) && c->num_tbs % nsm == 0 &&
+      (c->num_tbs / nsm == 2 || c->num_tbs / nsm == 4 || c->num_tbs / nsm == 8)) {
+    const int m = c->num_tbs / nsm;
+    cudaLaunchConfig_t lc = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)m;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    lc.gridDim = dim3((unsigned)c->num_tbs);
+    lc.blockDim = dim3((unsigned)c->threads);
+    lc.dynamicSmemBytes = smem;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    int fit = 0;
+    // groups never wait on one another, but a second wave of clusters doubles
+    // the time: clusters only when every group's cluster is resident at once
+    if (cudaOccupancyMaxActiveClusters(&fit, (const void*)fn, &lc) == cudaSuccess && fit >= nsm) cluster = m;
+    cudaGetLastError();
+  }
   if (is_barrier(c->prim)) {
     const int nb = c->num_tbs < nsm ? c->num_tbs : nsm;
     const int m = c->num_tbs / nb;

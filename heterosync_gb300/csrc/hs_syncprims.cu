@@ -26,34 +26,20 @@ namespace hs {
 // Mutex kernels: main.cu:317-529.  Global variants: one lock, every TB works on
 // chunk 0.  Uniq variants: lock and chunk per logical SM (blockIdx % NUM_SM).
 // ---------------------------------------------------------------------------
-template <int KIND, bool UNIQ, int MODE, int V, bool TMA = false>
-__global__ void __launch_bounds__(TMA ? 256 : Bounds<V>::kThreads) k_mutex(RunDesc d) {
-  __shared__ int s_slot;
-  __shared__ unsigned long long s_mbar;
-  extern __shared__ __align__(128) unsigned char dyn_smem[];
-  TmaCtx tma;
-  if constexpr (TMA) tma_init(tma, &s_mbar, dyn_smem);
-  const int b = blockIdx.x;
-  const int g = UNIQ ? (b % d.nsm) : 0;
-  unsigned* w0 = group_line(d, g, 0);
-  unsigned* w1 = group_line(d, g, 1);
-  unsigned* w2 = group_line(d, g, 2);
-  unsigned* ring = d.ring + (size_t)g * (d.ring_max + 1) * kRingStride;
-  const unsigned wrap = UNIQ ? 100000000u : 1000000000u;  // cudaLocksMutexFA.cu:24,83
-  const HsEnv env{d.status, d.timeout_ns};
-  // SLICE mode bookkeeping: group members b = g + r*G, r = 0..m-1.
-  const int G = UNIQ ? d.nsm : 1;
-  const int r = b / G;
-  const int m = (d.num_tbs - g + G - 1) / G;
-
+// One TB's iterations of a mutex kernel, at scope S (GPU: lock words in L2;
+// CLUSTER: lock words in the shared memory of the group's cluster rank 0).
+template <int S, int KIND, int MODE, int V, bool TMA>
+__device__ __forceinline__ void mutex_loop(const RunDesc& d, int g, int r, int m, int G, unsigned* w0, unsigned* w1,
+                                           unsigned* w2, unsigned* ring, unsigned ring_max, unsigned wrap,
+                                           int* s_slot, TmaCtx& tma, const HsEnv& env) {
   for (int j = 0; j < d.iters; ++j) {
     bool ok;
     int slot = 0;
-    if constexpr (KIND == MK_SPIN) ok = spin_lock<GPU>(w0, env);
-    else if constexpr (KIND == MK_EBO) ok = ebo_lock<GPU>(w0, d.bo_min, d.bo_max, env);
-    else if constexpr (KIND == MK_FA) ok = ticket_lock<GPU>(w0, w1, wrap, d.bo_unit, d.bo_max, env);
+    if constexpr (KIND == MK_SPIN) ok = spin_lock<S>(w0, env);
+    else if constexpr (KIND == MK_EBO) ok = ebo_lock<S>(w0, d.bo_min, d.bo_max, env);
+    else if constexpr (KIND == MK_FA) ok = ticket_lock<S>(w0, w1, wrap, d.bo_unit, d.bo_max, env);
     else {
-      slot = queue_lock<GPU>(w2, ring, kRingStride, d.ring_max, d.bo_unit, env, &s_slot);
+      slot = queue_lock<S>(w2, ring, kRingStride, ring_max, d.bo_unit, env, s_slot);
       ok = slot >= 0;
     }
     if (!ok) break;
@@ -62,36 +48,68 @@ __global__ void __launch_bounds__(TMA ? 256 : Bounds<V>::kThreads) k_mutex(RunDe
     else if constexpr (TMA) ok = cs_chunk_tma<MODE>(d, g, tma, env);
     else cs_chunk<MODE, V>(d, g);
 
-    if constexpr (KIND == MK_SPIN || KIND == MK_EBO) spin_unlock<GPU>(w0);
-    else if constexpr (KIND == MK_FA) ticket_unlock<GPU>(w1, wrap);
-    else queue_unlock<GPU>(ring, kRingStride, d.ring_max, (unsigned)slot);
+    if constexpr (KIND == MK_SPIN || KIND == MK_EBO) spin_unlock<S>(w0);
+    else if constexpr (KIND == MK_FA) ticket_unlock<S>(w1, wrap);
+    else queue_unlock<S>(ring, kRingStride, ring_max, (unsigned)slot);
     if (!ok) break;  // a bounded copy wait gave up (status already recorded)
   }
 }
 
 // ---------------------------------------------------------------------------
-// Semaphore kernels: main.cu:533-836.  One writer TB per logical SM
-// (perSM_blockID == smID % numTBs_perSM); the rest are readers.
+// Mutex kernels: main.cu:317-529.  Global variants: one lock, every TB works on
+// chunk 0.  Uniq variants: lock and chunk per logical SM (blockIdx % NUM_SM).
+// Uniq with d.cluster = m > 1 (numTBs = m * NUM_SM): each logical SM's group is
+// one thread-block cluster -- physical CTA p runs logical TB g + r*NUM_SM with
+// g = p / m, r = p % m -- and its lock lives in rank 0's shared memory, taken
+// and released with cluster-scope atomics on distributed shared memory.
 // ---------------------------------------------------------------------------
-template <bool EBO, bool UNIQ, int MODE, int V, bool TMA = false>
-__global__ void __launch_bounds__(TMA ? 256 : Bounds<V>::kThreads) k_sem(RunDesc d) {
+template <int KIND, bool UNIQ, int MODE, int V, bool TMA = false>
+__global__ void __launch_bounds__(TMA ? 256 : Bounds<V>::kThreads) k_mutex(RunDesc d) {
+  __shared__ int s_slot;
   __shared__ unsigned long long s_mbar;
   extern __shared__ __align__(128) unsigned char dyn_smem[];
   TmaCtx tma;
   if constexpr (TMA) tma_init(tma, &s_mbar, dyn_smem);
-  const int b = blockIdx.x;
-  const int Gd = d.num_tbs;
-  const int numSM = Gd < d.nsm ? Gd : d.nsm;
-  const int smID = b % numSM;
-  const int k = ceil_div(Gd, numSM);
-  const int p = b / numSM;
-  const bool writer = (p == smID % k);
-  unsigned* st = group_line(d, UNIQ ? smID : 0, 0);
+  const unsigned wrap = UNIQ ? 100000000u : 1000000000u;  // cudaLocksMutexFA.cu:24,83
   const HsEnv env{d.status, d.timeout_ns};
-  const int rchunk = UNIQ ? b : p;
+  if constexpr (UNIQ) {
+    if (d.cluster > 1) {
+      __shared__ unsigned s_cl_lock[3 * kLineWords];
+      __shared__ unsigned s_cl_ring[9 * kRingStride];
+      const int mc = d.cluster;
+      const int g = (int)blockIdx.x / mc, r = (int)blockIdx.x % mc;
+      if (r == 0) {  // the group's lock state, fresh for this launch (ring slot 0 holds the token)
+        for (int i = threadIdx.x; i < 3 * kLineWords; i += blockDim.x) s_cl_lock[i] = 0u;
+        for (int i = threadIdx.x; i < 9 * kRingStride; i += blockDim.x)
+          s_cl_ring[i] = (i % kRingStride) ? 0u : (i == 0 ? 1u : 0xFFFFFFFFu);
+      }
+      cluster_sync_all();
+      unsigned* lock0 = map_shared_rank(s_cl_lock, 0u);
+      mutex_loop<CLUSTER, KIND, MODE, V, TMA>(d, g, r, mc, d.nsm, lock0, lock0 + kLineWords, lock0 + 2 * kLineWords,
+                                              map_shared_rank(s_cl_ring, 0u), (unsigned)mc, wrap, &s_slot, tma,
+                                              env);
+      cluster_sync_all();  // rank 0's lock words stay valid until every rank is done
+      return;
+    }
+  }
+  const int b = blockIdx.x;
+  const int g = UNIQ ? (b % d.nsm) : 0;
+  // SLICE mode bookkeeping: group members b = g + r*G, r = 0..m-1.
+  const int G = UNIQ ? d.nsm : 1;
+  const int r = b / G;
+  const int m = (d.num_tbs - g + G - 1) / G;
+  mutex_loop<GPU, KIND, MODE, V, TMA>(d, g, r, m, G, group_line(d, g, 0), group_line(d, g, 1), group_line(d, g, 2),
+                                      d.ring + (size_t)g * (d.ring_max + 1) * kRingStride, d.ring_max, wrap, &s_slot,
+                                      tma, env);
+}
 
+// One TB's iterations of a semaphore kernel, at scope S.
+template <int S, bool EBO, bool UNIQ, int MODE, int V, bool TMA>
+__device__ __forceinline__ void sem_loop(const RunDesc& d, int b, int numSM, int k, bool writer, unsigned* st,
+                                         int rchunk, TmaCtx& tma, const HsEnv& env) {
+  const int Gd = d.num_tbs;
   for (int i = 0; i < d.iters; ++i) {
-    if (!sem_wait<GPU>(st, writer, d.sem_max, EBO, !UNIQ, d.bo_min, d.bo_max, env)) break;
+    if (!sem_wait<S>(st, writer, d.sem_max, EBO, !UNIQ, d.bo_min, d.bo_max, env)) break;
     bool ok = true;
     if (writer) {
       int cur = UNIQ ? b : 0;
@@ -104,9 +122,47 @@ __global__ void __launch_bounds__(TMA ? 256 : Bounds<V>::kThreads) k_sem(RunDesc
       if constexpr (TMA) ok = cs_read_tma(d, rchunk, tma, env, d.sink + b);
       else cs_read(d.data + (size_t)rchunk * chunk_words(d.T, d.L), d.T, d.L, d.sink + b);
     }
-    sem_post<GPU>(st, writer, d.sem_max);
+    sem_post<S>(st, writer, d.sem_max);
     if (!ok) break;
   }
+}
+
+// ---------------------------------------------------------------------------
+// Semaphore kernels: main.cu:533-836.  One writer TB per logical SM
+// (perSM_blockID == smID % numTBs_perSM); the rest are readers.  Uniq with
+// d.cluster = m > 1: as the Uniq mutexes, the group's semaphore word lives in
+// its cluster rank 0's shared memory.
+// ---------------------------------------------------------------------------
+template <bool EBO, bool UNIQ, int MODE, int V, bool TMA = false>
+__global__ void __launch_bounds__(TMA ? 256 : Bounds<V>::kThreads) k_sem(RunDesc d) {
+  __shared__ unsigned long long s_mbar;
+  extern __shared__ __align__(128) unsigned char dyn_smem[];
+  TmaCtx tma;
+  if constexpr (TMA) tma_init(tma, &s_mbar, dyn_smem);
+  const HsEnv env{d.status, d.timeout_ns};
+  const int Gd = d.num_tbs;
+  const int numSM = Gd < d.nsm ? Gd : d.nsm;
+  if constexpr (UNIQ) {
+    if (d.cluster > 1) {
+      __shared__ unsigned s_cl_sem[kLineWords];
+      const int mc = d.cluster;
+      const int smID = (int)blockIdx.x / mc, p = (int)blockIdx.x % mc;
+      const int b = smID + p * numSM;
+      if (p == 0 && threadIdx.x == 0) s_cl_sem[0] = d.sem_max;
+      cluster_sync_all();
+      sem_loop<CLUSTER, EBO, UNIQ, MODE, V, TMA>(d, b, numSM, mc, p == smID % mc, map_shared_rank(s_cl_sem, 0u), b,
+                                                 tma, env);
+      cluster_sync_all();
+      return;
+    }
+  }
+  const int b = blockIdx.x;
+  const int smID = b % numSM;
+  const int k = ceil_div(Gd, numSM);
+  const int p = b / numSM;
+  const bool writer = (p == smID % k);
+  sem_loop<GPU, EBO, UNIQ, MODE, V, TMA>(d, b, numSM, k, writer, group_line(d, UNIQ ? smID : 0, 0), UNIQ ? b : p,
+                                         tma, env);
 }
 
 // ---------------------------------------------------------------------------

@@ -142,3 +142,36 @@ def test_barrier_groups_on_clusters(hs, oracle, prim, mult, L):
         outs.append(st)
     want = oracle.golden(prim, 256, L, G, 4, 2, nsm, True, init)
     assert np.array_equal(outs[0], want) and np.array_equal(outs[1], want)
+
+
+@pytest.mark.parametrize("prim", [20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30, 31])
+@pytest.mark.parametrize("mult,L", [(2, 10), (4, 40), (8, 7)])
+@pytest.mark.parametrize("mode", ["inc", "ref"])
+def test_uniq_groups_on_clusters(hs, oracle, prim, mult, L, mode):
+    """Per-SM (Uniq) mutexes and semaphores with numTBs = mult * NUM_SM: each
+    group is one cluster and its lock word lives in distributed shared memory;
+    the result equals the flat launch's and the golden's."""
+    nsm = 16  # logical SMs: small groups keep the golden fast
+    G = mult * nsm
+    outs = []
+    for flags in (0, hs.RUN_NO_CLUSTER):
+        cfg = hs.RunConfig(prim=prim, num_ldst=L, num_tbs=G, num_iters=3, threads=64, repeats=2, mode=mode, nsm=nsm,
+                           flags=flags, timeout_ns=5_000_000_000)
+        init = _init(hs.storage_words(cfg), prim * 10 + mult)
+        st = init.copy()
+        res = hs.run(cfg, st)
+        # clusters when all nsm of them fit at once (always at 16 logical SMs)
+        assert res.status == 0 and res.cluster == (mult if flags == 0 else 1)
+        outs.append(st)
+    want = oracle.golden(prim, 64, L, G, 3, 2, nsm, mode == "inc", init)
+    assert np.array_equal(outs[0], want) and np.array_equal(outs[1], want)
+
+
+@pytest.mark.parametrize("prim", [20, 23])
+def test_uniq_slice_on_clusters(hs, oracle, prim):
+    cfg = hs.RunConfig(prim=prim, num_ldst=5, num_tbs=64, num_iters=4, threads=32, repeats=2, mode="slice", nsm=16)
+    init = _init(hs.storage_words(cfg), prim)
+    st = init.copy()
+    res = hs.run(cfg, st)
+    assert res.cluster == 4
+    assert np.array_equal(st, oracle.slice_replay(True, 5, 64, 4, 2, 16, init))
