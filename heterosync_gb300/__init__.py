@@ -43,7 +43,17 @@ PRIM_NAMES = {
     "spinSemUniq2": 25, "spinSemUniq10": 26, "spinSemUniq120": 27, "spinSemEBOUniq1": 28,
     "spinSemEBOUniq2": 29, "spinSemEBOUniq10": 30, "spinSemEBOUniq120": 31,
 }
-_ID_TO_NAME = {v: k for k, v in PRIM_NAMES.items()}
+# The HIP build's extra primitives (hip/syncPrims/uvm/main.hip.cpp:2056-2083):
+# priority semaphores and sense-reversing atomic tree barriers, run on the CUDA
+# primitive's kernel (hs_prim_base) with the same final storage.
+HIP_PRIM_NAMES = {
+    "PRspinSem1": 16, "PRspinSem2": 17, "PRspinSem10": 18, "PRspinSem120": 19,
+    "PRspinSemEBO1": 32, "PRspinSemEBO2": 33, "PRspinSemEBO10": 34, "PRspinSemEBO120": 35,
+    "atomicTreeBarrUniqSRB": 37, "atomicTreeBarrUniqLocalExchSRB": 38, "atomicTreeBarrUniqNaiveSRB": 39,
+    "atomicTreeBarrUniqLocalExchNaiveSRB": 40, "atomicTreeBarrUniqNaiveAllSRB": 41,
+    "atomicTreeBarrUniqLocalExchNaiveAllSRB": 42,
+}
+_ID_TO_NAME = {v: k for k, v in list(PRIM_NAMES.items()) + list(HIP_PRIM_NAMES.items())}
 
 
 class HsError(RuntimeError):
@@ -130,9 +140,19 @@ def prim_id(name) -> int:
         if name not in _ID_TO_NAME:
             raise ValueError("unknown syncPrim id %d" % name)
         return name
-    if name not in PRIM_NAMES:
-        raise ValueError("ERROR: Unknown synchronization primitive: %s" % name)
-    return PRIM_NAMES[name]
+    if name in PRIM_NAMES:
+        return PRIM_NAMES[name]
+    if name in HIP_PRIM_NAMES:
+        return HIP_PRIM_NAMES[name]
+    raise ValueError("ERROR: Unknown synchronization primitive: %s" % name)
+
+
+def prim_base(prim) -> tuple:
+    """(CUDA base primitive id, variant) a primitive runs as."""
+    v = ctypes.c_int()
+    lib().hs_prim_base.argtypes = [ctypes.c_int, ctypes.c_void_p]
+    b = lib().hs_prim_base(prim_id(prim), ctypes.byref(v))
+    return b, v.value
 
 
 def prim_name(pid: int) -> str:
@@ -652,8 +672,8 @@ class _BatchResult(ctypes.Structure):
                 ("failed_instance", ctypes.c_int)]
 
 
-BATCH_REFCOUNTER, BATCH_SPLITCOUNTER, BATCH_SEQLOCK, BATCH_FLAGS = 40, 41, 42, 43
-BATCH_KIND_NAMES = {40: "RefCounter", 41: "SplitCounter", 42: "Seqlock", 43: "Flags"}
+BATCH_REFCOUNTER, BATCH_SPLITCOUNTER, BATCH_SEQLOCK, BATCH_FLAGS = 60, 61, 62, 63
+BATCH_KIND_NAMES = {60: "RefCounter", 61: "SplitCounter", 62: "Seqlock", 63: "Flags"}
 
 
 def batch_instance_words(inst, nsm: int = 0) -> int:

@@ -54,7 +54,10 @@ static void usage() {
                "\t\tspinSemEBOUniq1 - Spin Semaphore with Backoff (Max: 1) -- accesses to unique locations per TB\n"
                "\t\tspinSemEBOUniq2 - Spin Semaphore with Backoff (Max: 2) -- accesses to unique locations per TB\n"
                "\t\tspinSemEBOUniq10 - Spin Semaphore with Backoff (Max: 10) -- accesses to unique locations per TB\n"
-               "\t\tspinSemEBOUniq120 - Spin Semaphore with Backoff (Max: 120) -- accesses to unique locations per TB\n");
+               "\t\tspinSemEBOUniq120 - Spin Semaphore with Backoff (Max: 120) -- accesses to unique locations per TB\n"
+               "\tAlso accepted (the HIP build's extra primitives):\n"
+               "\t\tPRspinSem{1,2,10,120}, PRspinSemEBO{1,2,10,120} - Priority Spin Semaphores\n"
+               "\t\tatomicTreeBarrUniq[LocalExch]{SRB,NaiveSRB,NaiveAllSRB} - Sense Reversing Barriers\n");
   std::fprintf(stderr, "\t<numLdSt>: the # of LDs and STs to do for each thread in the critical section.\n");
   std::fprintf(stderr, "\t<numTBs>: the # of TBs to execute (want to be divisible by the number of SMs).\n");
   std::fprintf(stderr, "\t<numCSIters>: number of iterations of the critical section.\n");

@@ -110,7 +110,49 @@ static const PrimInfo kPrims[] = {
     {29, "spinSemEBOUniq2", "ebo_sem_uniq_%03d_%03d", 2, 2},
     {30, "spinSemEBOUniq10", "ebo_sem_uniq_%03d_%03d", 10, 10},
     {31, "spinSemEBOUniq120", "ebo_sem_uniq_%03d_%03d", 120, 120},
+    // HIP build only (hip/syncPrims/uvm/main.hip.cpp:2056-2083 names, 2240-2338 labels)
+    {16, "PRspinSem1", "prior_spin_lock_sem_%03d_%03d", 1, 1},
+    {17, "PRspinSem2", "prior_spin_lock_sem_%03d_%03d", 2, 2},
+    {18, "PRspinSem10", "prior_spin_lock_sem_%03d_%03d", 10, 10},
+    {19, "PRspinSem120", "prior_spin_lock_sem_%03d_%03d", 2, 120},
+    {32, "PRspinSemEBO1", "prior_ebo_sem_%03d_%03d", 1, 1},
+    {33, "PRspinSemEBO2", "prior_ebo_sem_%03d_%03d", 2, 2},
+    {34, "PRspinSemEBO10", "prior_ebo_sem_%03d_%03d", 10, 10},
+    {35, "PRspinSemEBO120", "prior_ebo_sem_%03d_%03d", 120, 120},
+    {37, "atomicTreeBarrUniqSRB", "atomic_tree_barrier_SRB_%03d", 0, 0},
+    {38, "atomicTreeBarrUniqLocalExchSRB", "atomic_tree_barrier_localExch_SRB_%03d", 0, 0},
+    {39, "atomicTreeBarrUniqNaiveSRB", "atomic_tree_barrier_NaiveSRB_%03d", 0, 0},
+    {40, "atomicTreeBarrUniqLocalExchNaiveSRB", "atomic_tree_barrier_localExch_NaiveSRB_%03d", 0, 0},
+    {41, "atomicTreeBarrUniqNaiveAllSRB", "atomic_tree_barrier_NaiveAllSRB_%03d", 0, 0},
+    {42, "atomicTreeBarrUniqLocalExchNaiveAllSRB", "atomic_tree_barrier_localExch_NaiveAllSRB_%03d", 0, 0},
 };
+
+// The CUDA primitive a HIP-extension id runs, and its variant.
+static int canon_prim(int prim, int* variant) {
+  *variant = PV_NONE;
+  if (prim >= 16 && prim <= 19) { *variant = PV_PRIORITY; return prim - 8; }   // -> spinSem*
+  if (prim >= 32 && prim <= 35) { *variant = PV_PRIORITY; return prim - 20; }  // -> spinSemEBO*
+  if (prim >= 37 && prim <= 42) {
+    static const int v[6] = {PV_SRB, PV_SRB, PV_NAIVE, PV_NAIVE, PV_NAIVE_ALL, PV_NAIVE_ALL};
+    *variant = v[prim - 37];
+    return (prim - 37) % 2;  // -> atomicTreeBarrUniq(LocalExch)
+  }
+  return prim;
+}
+
+// A copy of the configuration with the primitive replaced by its CUDA base.
+static const hs_run_config* canon(const hs_run_config* c, hs_run_config* tmp, int* variant) {
+  if (!c) return c;
+  *tmp = *c;
+  tmp->prim = canon_prim(c->prim, variant);
+  return tmp;
+}
+extern "C" int hs_prim_base(int prim, int* variant) {
+  int v = 0;
+  const int b = canon_prim(prim, &v);
+  if (variant) *variant = v;
+  return b;
+}
 static const PrimInfo* find_prim(int id) {
   for (const auto& p : kPrims)
     if (p.id == id) return &p;
@@ -184,7 +226,10 @@ static int validate(const hs_run_config* c, int nsm) {
   return HS_OK;
 }
 
-extern "C" int hs_storage_words(const hs_run_config* c, int nsm, size_t* words) {
+extern "C" int hs_storage_words(const hs_run_config* c0, int nsm, size_t* words) {
+  hs_run_config tmp;
+  int variant = 0;
+  const hs_run_config* c = canon(c0, &tmp, &variant);
   nsm = device_nsm(nsm > 0 ? nsm : (c ? c->nsm : 0));
   int v = validate(c, nsm);
   if (v) return v;
@@ -244,8 +289,11 @@ static void shift_counts(const hs_run_config* c, int nsm, std::vector<unsigned l
   }
 }
 
-extern "C" int hs_expected_storage(const hs_run_config* c, int nsm, const uint32_t* init, uint32_t* out,
+extern "C" int hs_expected_storage(const hs_run_config* c0, int nsm, const uint32_t* init, uint32_t* out,
                                    size_t words) {
+  hs_run_config tmp;
+  int variant = 0;
+  const hs_run_config* c = canon(c0, &tmp, &variant);
   nsm = device_nsm(nsm > 0 ? nsm : (c ? c->nsm : 0));
   int v = validate(c, nsm);
   if (v) return v;
@@ -435,9 +483,12 @@ static int read_status(hs_ctx* ctx, cudaStream_t st, hs_run_result* r) {
   return HS_OK;
 }
 
-extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c, void* storage, int on_device, void* stream,
+extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c0, void* storage, int on_device, void* stream,
                       hs_run_result* r) {
-  if (!ctx || !c || !storage || !r) { g_err = "null argument"; return HS_EINVAL; }
+  if (!ctx || !c0 || !storage || !r) { g_err = "null argument"; return HS_EINVAL; }
+  hs_run_config tmp;
+  int variant = 0;
+  const hs_run_config* c = canon(c0, &tmp, &variant);
   std::memset(r, 0, sizeof(*r));
   const int nsm = c->nsm > 0 ? c->nsm : ctx->nsm;
   int s = validate(c, nsm);
@@ -482,7 +533,8 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c, void* storage, int on
   if (is_barrier(c->prim)) {
     const int nb = c->num_tbs < nsm ? c->num_tbs : nsm;
     const int m = c->num_tbs / nb;
-    if (!(c->flags & HS_RUN_NO_CLUSTER) && c->skip_tb < 0 && c->num_tbs % nb == 0 && (m == 2 || m == 4 || m == 8)) {
+    if (!(c->flags & HS_RUN_NO_CLUSTER) && c->skip_tb < 0 && c->num_tbs % nb == 0 && (m == 2 || m == 4 || m == 8) &&
+        variant != PV_NAIVE && variant != PV_NAIVE_ALL) {
       cudaLaunchConfig_t lc = {};
       cudaLaunchAttribute attr[1];
       attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -521,6 +573,7 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c, void* storage, int on
   if ((s = hs_prepare_run(ctx, c, nsm, dev, st, &d, !(c->flags & HS_RUN_KEEP_STATE)))) return r->status = s;
 
   d.cluster = cluster;
+  d.variant = variant;
   r->cluster = cluster;
   cudaLaunchConfig_t lc = {};
   cudaLaunchAttribute attr[1];
@@ -639,7 +692,10 @@ extern "C" int cudaSemaphoreCreateEBO(unsigned int* const h, const int s, const 
 
 // Lock-state layout of a run, for entry points that place the state in memory
 // they do not allocate here.
-int hs_layout_for(const hs_run_config* c, int nsm, hs::Layout* out) {
+int hs_layout_for(const hs_run_config* c0, int nsm, hs::Layout* out) {
+  hs_run_config tmp;
+  int variant = 0;
+  const hs_run_config* c = canon(c0, &tmp, &variant);
   *out = make_layout(c, nsm);
   return HS_OK;
 }

@@ -198,7 +198,7 @@ __device__ __noinline__ void batch_barrier(const RunDesc& d, int rank, int c, un
 //                  the flag and count data words below it (flags_kernel.cu
 //                  stop/dirty message passing, without waiting).
 // ---------------------------------------------------------------------------
-enum : int { P_REFCOUNT = 40, P_SPLITCOUNT = 41, P_SEQLOCK = 42, P_FLAGS = 43 };
+enum : int { P_REFCOUNT = 60, P_SPLITCOUNT = 61, P_SEQLOCK = 62, P_FLAGS = 63 };
 __device__ __forceinline__ bool is_relaxed_prim(int p) { return p >= P_REFCOUNT && p <= P_FLAGS; }
 
 __device__ __forceinline__ unsigned long long seq_pattern(unsigned seq, int i) {

@@ -49,6 +49,19 @@ struct RunDesc {
   int l_grp;            // per-group lines: 4 per group
   int l_lflag;          // per-group member flags (dense), lflag_lines per group
   int lflag_lines;
+  int variant;          // HIP-extension variant of the primitive (PrimVariant)
+};
+
+// Variants the HIP build of the reference adds to the CUDA primitives
+// (hip/syncPrims/uvm/main.hip.cpp:2040-2090): they run the CUDA primitive's
+// kernel with the variant's barrier form; the critical sections, and so the
+// final storage, are the CUDA primitive's.
+enum PrimVariant : int {
+  PV_NONE = 0,
+  PV_PRIORITY = 1,   // PRspinSem*, PRspinSemEBO*: exiting TBs go first
+  PV_SRB = 2,        // atomicTreeBarrUniq*SRB: sense-reversing tree barrier
+  PV_NAIVE = 3,      // *NaiveSRB: every TB joins one global barrier (no local stage)
+  PV_NAIVE_ALL = 4,  // *NaiveAllSRB: every thread joins one global barrier
 };
 
 // Lock-state layout for a run: line offsets and total size.

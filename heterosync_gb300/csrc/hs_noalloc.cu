@@ -76,9 +76,15 @@ size_t round64(size_t w) { return (w + 63) / 64 * 64; }  // 256-byte granules
 
 extern "C" const char* hs_noalloc_last_error(void) { return g_noalloc_err; }
 
-extern "C" int hs_run_noalloc(const hs_run_config* c, void* storage, void* stream, hs_run_result* r) {
+extern "C" int hs_prim_base(int prim, int* variant);
+
+extern "C" int hs_run_noalloc(const hs_run_config* c0, void* storage, void* stream, hs_run_result* r) {
   using namespace hs;
-  if (!c || !storage || !r) { set_err("null argument"); return HS_EINVAL; }
+  if (!c0 || !storage || !r) { set_err("null argument"); return HS_EINVAL; }
+  hs_run_config cc = *c0;  // a HIP-extension id runs its CUDA base primitive (variant below)
+  int variant = 0;
+  cc.prim = hs_prim_base(c0->prim, &variant);
+  const hs_run_config* c = &cc;
   std::memset(r, 0, sizeof(*r));
   r->cluster = 1;
   int dev = 0, nsm = c->nsm;
@@ -131,6 +137,7 @@ extern "C" int hs_run_noalloc(const hs_run_config* c, void* storage, void* strea
   d.sink = d.ring + w_ring;
   d.data = static_cast<unsigned*>(storage);
   d.prim = c->prim;
+  d.variant = variant;
   d.mode = c->mode;
   d.T = c->threads;
   d.L = c->num_ldst;

@@ -287,6 +287,24 @@ __device__ __forceinline__ unsigned dyn_smem_bytes_b() {
   return r;
 }
 
+// The HIP build's naive sense-reversing barriers (hip/syncPrims/uvm/
+// main.hip.cpp:238-302, 434-530): no local stage; every TB (PV_NAIVE) or every
+// thread (PV_NAIVE_ALL) joins one global counter barrier.
+__device__ __forceinline__ bool flat_barrier(const RunDesc& d, BarState& s, const HsEnv& env, bool all_threads) {
+  unsigned* gcount = d.locks + (size_t)(d.l_glob + 0) * kLineWords;
+  unsigned* ggenw = d.locks + (size_t)(d.l_glob + 1) * kLineWords;
+  __syncthreads();  // every thread's critical-section stores precede the arrival
+  int ok = 1;
+  if (all_threads || is_master()) {
+    bool okb = true;
+    const unsigned n = all_threads ? (unsigned)d.num_tbs * blockDim.x : (unsigned)d.num_tbs;
+    counter_barrier<GPU>(gcount, ggenw, n, s.ggen, d.bo_unit, env, HS_SITE_BAR_GLOBAL, [] { return true; }, &okb);
+    ok = okb;
+  }
+  s.ggen += 1u;
+  return __syncthreads_or(!ok) == 0;
+}
+
 // Tree barrier with the local stage on a thread-block cluster: the group's
 // members are the cluster's CTAs.  Local arrival and local release are the
 // hardware cluster barrier; between them the leader (rank 0) runs the global
@@ -355,6 +373,7 @@ __global__ void __launch_bounds__(TMA ? 256 : Bounds<V>::kThreads, TMA ? 4 : 102
   const int Gd = d.num_tbs;
   const int nb = Gd < d.nsm ? Gd : d.nsm;
   const bool clustered = d.cluster > 1;
+  const bool naive = !LF && (d.variant == PV_NAIVE || d.variant == PV_NAIVE_ALL);
   const int g = clustered ? (int)blockIdx.x / d.cluster : (int)blockIdx.x % nb;
   const int r = clustered ? (int)blockIdx.x % d.cluster : (int)blockIdx.x / nb;
   const int b = g + r * nb;
@@ -381,16 +400,24 @@ __global__ void __launch_bounds__(TMA ? 256 : Bounds<V>::kThreads, TMA ? 4 : 102
     // numBlocksAtBarr TBs ahead (one call site keeps one inlined copy of the CS)
     for (int ph = 0; ph < phases; ++ph) {
       if (ph == 1) {
-        if (clustered) cluster_sync_all();
-        else if (!local_only_barrier<LF>(d, g, r, m, s, env)) return;
+        if (naive) {  // no local stage: the naive barriers join the global one here
+          if (!flat_barrier(d, s, env, d.variant == PV_NAIVE_ALL)) return;
+        } else if (clustered) {
+          cluster_sync_all();
+        } else if (!local_only_barrier<LF>(d, g, r, m, s, env)) {
+          return;
+        }
         cur = (cur + nb) % Gd;
       }
       if constexpr (TMA) cs_chunk_tma_tiled<MODE>(d, cur, tma, tma.cap, env);
       else cs_chunk<MODE, V>(d, cur);
       if (b == d.skip_tb) return;  // fault injection: this TB never arrives (never in cluster mode)
     }
-    if (clustered ? !cluster_tree_barrier<LF>(d, g, r, nb, s, env) : !tree_barrier<LF>(d, g, r, m, nb, s, env))
+    if (naive) {
+      if (!flat_barrier(d, s, env, d.variant == PV_NAIVE_ALL)) return;
+    } else if (clustered ? !cluster_tree_barrier<LF>(d, g, r, nb, s, env) : !tree_barrier<LF>(d, g, r, m, nb, s, env)) {
       return;
+    }
     cur = (cur + 1) % Gd;
   }
 }

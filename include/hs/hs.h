@@ -102,6 +102,11 @@ const char* hs_prim_name(int prim);
 int hs_prim_label(int prim, int num_iters, char* buf, int buflen);
 /* Semaphore size for semaphore prims (1, 2, 10, 120), 0 otherwise. */
 int hs_prim_sem_count(int prim);
+/* The CUDA primitive a HIP-build-only id runs (PRspinSem* -> spinSem*,
+ * PRspinSemEBO* -> spinSemEBO*, atomicTreeBarrUniq*SRB -> atomicTreeBarrUniq(LocalExch)),
+ * and its variant (1 priority, 2 sense-reversing tree, 3 naive, 4 naive all
+ * threads); other ids map to themselves, variant 0. */
+int hs_prim_base(int prim, int* variant);
 /* Storage words a run needs (numLocsMult * threads * (numLdSt+1), main.cu:1283-1308;
  * numTBs * numLdSt for HS_MODE_SLICE). */
 int hs_storage_words(const hs_run_config* cfg, int nsm, size_t* words);
@@ -145,7 +150,7 @@ typedef struct hs_batch_instance { int prim, num_ldst, num_tbs, num_iters; } hs_
  * microbenchmarks at instance scale (refCounter_kernel.cu, splitCounter_kernel.cu,
  * seqlocks_kernel.cu, flags_kernel.cu); 256 threads per TB, numLdSt sets the
  * counter / data width. */
-enum { HS_BATCH_REFCOUNTER = 40, HS_BATCH_SPLITCOUNTER = 41, HS_BATCH_SEQLOCK = 42, HS_BATCH_FLAGS = 43 };
+enum { HS_BATCH_REFCOUNTER = 60, HS_BATCH_SPLITCOUNTER = 61, HS_BATCH_SEQLOCK = 62, HS_BATCH_FLAGS = 63 };
 int hs_batch_instance_words(const hs_batch_instance* inst, int nsm, size_t* words);
 /* Closed-form final storage of one instance after one run (mode: HS_MODE_INC or HS_MODE_REF). */
 int hs_batch_expected_storage(const hs_batch_instance* inst, int nsm, int mode, const uint32_t* init,

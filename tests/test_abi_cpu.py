@@ -79,3 +79,30 @@ def test_status_strings(hs):
     assert L.hs_status_string(0) == b"ok"
     assert L.hs_status_string(2) == b"device wait timed out"
     assert L.hs_version() >= 1
+
+
+def test_hip_extension_names_and_bases(hs):
+    """The HIP build's extra primitives (main.hip.cpp:2056-2083) resolve by name,
+    print the HIP labels and run as their CUDA base primitive."""
+    L = hs.lib()
+    for name, pid in hs.HIP_PRIM_NAMES.items():
+        assert L.hs_prim_id(name.encode()) == pid
+    assert hs.prim_base("PRspinSem10") == (10, 1)
+    assert hs.prim_base("PRspinSemEBO120") == (15, 1)
+    assert hs.prim_base("atomicTreeBarrUniqSRB") == (0, 2)
+    assert hs.prim_base("atomicTreeBarrUniqLocalExchNaiveSRB") == (1, 3)
+    assert hs.prim_base("atomicTreeBarrUniqLocalExchNaiveAllSRB") == (1, 4)
+    assert hs.prim_base("faMutex") == (7, 0)
+    assert hs.prim_label("PRspinSem120", 10) == "prior_spin_lock_sem_002_010"
+    assert hs.prim_label("PRspinSemEBO2", 10) == "prior_ebo_sem_002_010"
+    assert hs.prim_label("atomicTreeBarrUniqLocalExchNaiveAllSRB", 5) == "atomic_tree_barrier_localExch_NaiveAllSRB_005"
+
+
+def test_hip_extension_storage_and_closed_form(hs):
+    for name, base in [("PRspinSem2", "spinSem2"), ("atomicTreeBarrUniqNaiveSRB", "atomicTreeBarrUniq"),
+                       ("atomicTreeBarrUniqLocalExchSRB", "atomicTreeBarrUniqLocalExch")]:
+        a = hs.RunConfig(prim=name, num_ldst=7, num_tbs=24, num_iters=3, threads=64, repeats=2, mode="inc", nsm=8)
+        b = hs.RunConfig(prim=base, num_ldst=7, num_tbs=24, num_iters=3, threads=64, repeats=2, mode="inc", nsm=8)
+        assert hs.storage_words(a) == hs.storage_words(b)
+        init = np.arange(hs.storage_words(a), dtype=np.uint32)
+        assert np.array_equal(hs.expected_storage(a, init), hs.expected_storage(b, init))

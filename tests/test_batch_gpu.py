@@ -34,7 +34,7 @@ def _run_both(hs, insts, mode="inc"):
 def test_every_primitive_once(hs):
     insts = [(p, 7 + (p % 5) * 9, 3 + p % 13, 6 + p % 4) for p in
              [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30, 31,
-              40, 41, 42, 43]]
+              60, 61, 62, 63]]
     rs, rb, v = _run_both(hs, insts)
     assert rb.grid > 0 and rb.ops == rs.ops
     assert rs.launches >= len(insts)
@@ -87,7 +87,7 @@ def test_cluster_plans_bit_exact(hs, cl, mode):
 
 
 
-@pytest.mark.parametrize("kind", [40, 41, 42, 43])
+@pytest.mark.parametrize("kind", [60, 61, 62, 63])
 def test_relaxed_kinds(hs, kind):
     """RefCounter, SplitCounter, Seqlock (4 x u64 payload) and Flags instances:
     final counters, payload and data exact, no torn seqlock read and no flag

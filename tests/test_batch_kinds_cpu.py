@@ -61,7 +61,7 @@ def test_flags(hs, L, G, I):
 def test_generator_draws_every_kind(hs):
     insts = hs.batch_generate(seed=20260101, n=512, nsm=NSM)
     kinds = {p for p, _, _, _ in insts}
-    assert {40, 41, 42, 43} <= kinds and len(kinds) == 32
+    assert {60, 61, 62, 63} <= kinds and len(kinds) == 32
 
 
 def test_syncprims_expected_matches_run_config_form(hs):

@@ -19,3 +19,12 @@ def test_usage_lists_all_primitives(hs):
     assert r.returncode == 255
     for name in hs.PRIM_NAMES:
         assert "\t\t%s - " % name in r.stderr
+
+
+def test_usage_lists_hip_extensions():
+    import os
+    import subprocess
+    exe = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "heterosync_gb300", "bin",
+                       "allSyncPrims-1kernel")
+    p = subprocess.run([exe], capture_output=True, text=True)
+    assert p.returncode != 0 and "PRspinSem" in p.stderr and "NaiveAllSRB" in p.stderr

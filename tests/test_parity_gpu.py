@@ -175,3 +175,23 @@ def test_uniq_slice_on_clusters(hs, oracle, prim):
     res = hs.run(cfg, st)
     assert res.cluster == 4
     assert np.array_equal(st, oracle.slice_replay(True, 5, 64, 4, 2, 16, init))
+
+
+@pytest.mark.parametrize("name,base", [("PRspinSem1", 8), ("PRspinSem120", 11), ("PRspinSemEBO2", 13),
+                                       ("PRspinSemEBO10", 14), ("atomicTreeBarrUniqSRB", 0),
+                                       ("atomicTreeBarrUniqLocalExchSRB", 1), ("atomicTreeBarrUniqNaiveSRB", 0),
+                                       ("atomicTreeBarrUniqLocalExchNaiveSRB", 1),
+                                       ("atomicTreeBarrUniqNaiveAllSRB", 0),
+                                       ("atomicTreeBarrUniqLocalExchNaiveAllSRB", 1)])
+@pytest.mark.parametrize("mode", ["ref", "inc"])
+def test_hip_extension_primitives(hs, oracle, name, base, mode):
+    """The HIP build's priority semaphores and sense-reversing barriers: the
+    final storage is the CUDA base primitive's golden."""
+    for ci, (T, L, G, iters, reps, nsm) in enumerate(CASES[:4]):
+        cfg = hs.RunConfig(prim=name, num_ldst=L, num_tbs=G, num_iters=iters, threads=T, repeats=reps, mode=mode,
+                           nsm=nsm, timeout_ns=5_000_000_000)
+        init = _init(hs.storage_words(cfg), base * 7 + ci)
+        st = init.copy()
+        res = hs.run(cfg, st)
+        assert res.status == 0
+        assert np.array_equal(st, oracle.golden(base, T, L, G, iters, reps, nsm, mode == "inc", init)), (name, ci)
