@@ -503,6 +503,16 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c0, void* storage, int o
   size_t smem = 0;
   KernelFn fn = syncprim_plan(c->prim, c->mode, c->threads, c->num_ldst, &smem, !(c->flags & HS_RUN_REGISTER_CS));
   if (!fn) { g_err = "no kernel for this primitive/mode"; return r->status = HS_EINVAL; }
+  if (is_barrier(c->prim) && smem > 0) {
+    // bulk-copy tiles: the shared memory the co-resident TBs of one SM leave
+    // free (one TB per SM takes a whole chunk, four take 48 KB tiles)
+    const size_t chunk = (size_t)c->threads * (c->num_ldst + 1) * 4;
+    const size_t region = (size_t)64 * (c->num_ldst + 1);
+    const int per_sm = (c->num_tbs + ctx->nsm - 1) / ctx->nsm;
+    size_t budget = per_sm > 0 ? (size_t)(216 * 1024) / (size_t)per_sm : smem;
+    budget = std::min(budget, (size_t)(200 * 1024)) / region * region;  // the bulk-copy path's cap
+    smem = std::max(smem, std::min(chunk, budget));
+  }
   HS_CK(prepare_smem(fn, smem));
   // Tree barriers whose logical-SM groups are all the same size (numTBs a
   // multiple of NUM_SM, 2 to 8 per group) run each group as one thread-block
