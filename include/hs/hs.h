@@ -166,7 +166,7 @@ typedef struct hs_batch_result {
 } hs_batch_result;
 typedef struct hs_batch hs_batch;
 const char* hs_batch_last_error(void);
-/* The mixed batch of BASELINE config 4, drawn from std::mt19937_64(seed). */
+/* The mixed batch (32 kinds), drawn from std::mt19937_64(seed). */
 int hs_batch_generate(unsigned long long seed, int n, int nsm, int iter_div, hs_batch_instance* out);
 int hs_batch_create(const hs_batch_instance* inst, int n, int threads, int mode, hs_batch** out);
 int hs_batch_destroy(hs_batch* b);

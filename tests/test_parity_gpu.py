@@ -17,7 +17,7 @@ ALL_PRIMS = [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15,
 # (threads, numLdSt, numTBs, iters, repeats, nsm): even group sizes
 CASES = [
     (32, 40, 8, 2, 2, 4),     # 2 TBs per logical SM, multi-pass shift (40 > 32 lines)
-    (256, 10, 6, 1, 1, 3),    # BASELINE thread count
+    (256, 10, 6, 1, 1, 3),    # 256 threads per TB
     (64, 25, 5, 2, 1, 8),     # fewer TBs than SMs
     (16, 12, 12, 1, 1, 4),    # 3 TBs per logical SM, half-warp TBs
     (256, 100, 4, 2, 1, 2),   # 100 KB chunks: bulk-copy (TMA) critical sections
@@ -48,7 +48,7 @@ def test_parity_host_storage(hs, oracle, prim, mode):
 
 @pytest.mark.parametrize("prim", [4, 5, 6, 7, 20, 21, 22, 23])
 def test_slice_mode(hs, oracle, prim):
-    """BASELINE workload: uint32[numTBs*numLdSt] seeded in [0,1000), +1 per critical section."""
+    """The slice workload: uint32[numTBs*numLdSt] seeded in [0,1000), +1 per critical section."""
     for (T, L, G, iters, reps, nsm) in [(256, 10, 8, 100, 1, 0), (64, 7, 24, 20, 2, 4), (32, 33, 17, 9, 1, 5)]:
         cfg = hs.RunConfig(prim=prim, num_ldst=L, num_tbs=G, num_iters=iters, threads=T, repeats=reps,
                            mode="slice", nsm=nsm)
