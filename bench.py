@@ -25,7 +25,8 @@ CTA rotated every episode, 1000 episodes, cluster sizes 1/2/4/8) and "batch"
 (the 64-instance mixed batch, one launch per instance against the autotuned
 persistent graph-replayed launch) and "serve" (the served request loop: peak
 request rate, p50/p99 latency under Poisson arrivals at 10-90% of it) and
-"uts_geo" (geometric SHA-1 UTS, depth 12, nodes/s); the
+"uts_geo" (geometric SHA-1 UTS, depth 12, nodes/s, on the GPU alone and
+with the host cores walking the same tree cooperatively); the
 extras run outside the sweep's timed region; --no-extras skips them.
 
 --impl reference runs the reference's own SyncPrims kernels (built from its
@@ -352,8 +353,22 @@ def uts_geo_extra(hs):
     t0 = time.perf_counter()
     oracle.geo_count(2, 9)
     host_s = time.perf_counter() - t0
+    coop = {}
+    for seed in (2, 3):  # the same trees walked by the GPU CTAs and the host cores together
+        try:
+            r = hs.uts_geo_coop_run(seed, 12, 4.0, blocks=304, threads=256, host_threads=-1)
+        except hs.HsError as e:
+            coop = {"unavailable": str(e)}
+            break
+        if (r["nodes"], r["leaves"], r["max_depth"]) != (rows["seed%d" % seed]["nodes"], rows["seed%d" % seed]["leaves"],
+                                                         rows["seed%d" % seed]["deepest"]):
+            raise SystemExit("bench: cooperative UTS counts differ from the GPU walk")
+        coop["seed%d" % seed] = {"ms": round(r["elapsed_ms"], 3), "nodes_per_s": r["nodes"] / (r["elapsed_ms"] * 1e-3),
+                                 "host_share": r["host_nodes"] / r["nodes"], "host_threads": r["host_threads"],
+                                 "to_host": r["to_host"], "to_gpu": r["to_gpu"]}
     return {"workload": "geometric tree, SHA-1 node generator, branching 4, depth limit 12, 304 CTAs x 256",
-            "results": rows, "check": "depth 9, seed 2: %d nodes, equal to the host walk" % want[0],
+            "results": rows, "cooperative": coop,
+            "check": "depth 9, seed 2: %d nodes, equal to the host walk" % want[0],
             "cpu_baseline": {"nodes_per_s": want[0] / host_s, "cores": 1, "kind": "port",
                              "sample": "host depth-first walk of seed 2 at depth 9 (%d nodes)" % want[0]}}
 

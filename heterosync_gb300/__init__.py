@@ -453,6 +453,33 @@ def uts_geo_run(seed: int, depth_limit: int, branching: float = 4.0, blocks: int
     return r.nodes, r.leaves, r.max_depth, r.elapsed_ms
 
 
+class _CoopResult(ctypes.Structure):
+    _fields_ = [("nodes", ctypes.c_ulonglong), ("leaves", ctypes.c_ulonglong), ("max_depth", ctypes.c_uint),
+                ("gpu_nodes", ctypes.c_ulonglong), ("host_nodes", ctypes.c_ulonglong),
+                ("to_host", ctypes.c_ulonglong), ("to_gpu", ctypes.c_ulonglong), ("host_threads", ctypes.c_int),
+                ("elapsed_ms", ctypes.c_float), ("dev_error_bits", ctypes.c_uint)]
+
+
+def uts_geo_coop_run(seed: int, depth_limit: int, branching: float = 4.0, blocks: int | None = None,
+                     threads: int = 256, host_threads: int = -1, timeout_ns: int = 0) -> dict:
+    """Walk the geometric tree with GPU CTAs and host threads together
+    (hs_uts_geo_coop_run).  blocks None: 2 CTAs per SM; blocks 0: host threads
+    only (no CUDA call).  host_threads -1: the host's cores minus one.
+    Returns the counts, each side's share and the items that crossed the link."""
+    if blocks is None:
+        blocks = device_info()["nsm"] * 2
+    r = _CoopResult()
+    L = lib()
+    L.hs_uts_geo_last_error.restype = ctypes.c_char_p
+    L.hs_uts_geo_coop_run.argtypes = [ctypes.c_uint, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_int, ctypes.c_ulonglong, ctypes.c_void_p]
+    s = L.hs_uts_geo_coop_run(seed, depth_limit, branching, blocks, threads, host_threads, timeout_ns,
+                              ctypes.byref(r))
+    if s:
+        raise HsError(s, L.hs_uts_geo_last_error().decode())
+    return {f: getattr(r, f) for f, _ in _CoopResult._fields_}
+
+
 # ---------------------------------------------------------------------------
 # Tree barrier with local exchange on thread-block clusters (hs_exchange_*)
 # ---------------------------------------------------------------------------

@@ -11,7 +11,7 @@
       each offered load; p50/p99 latency, throughput, the offline batch of the
       same requests, bit-exact check of every result
 
-  python -m heterosync_gb300.cli uts-geo [--seed 2] [--depth 12]
+  python -m heterosync_gb300.cli uts-geo [--seed 2] [--depth 12] [--host-threads N]
          [--branching 4] [--blocks 304] [--threads 256]
       geometric SHA-1 UTS by work stealing; node, leaf and depth counts
 
@@ -88,7 +88,15 @@ def cmd_batch(a):
 
 
 def cmd_uts_geo(a):
-    from . import uts_geo_run
+    from . import uts_geo_coop_run, uts_geo_run
+    if a.host_threads is not None:  # cooperative: GPU CTAs and host threads on one tree
+        r = uts_geo_coop_run(a.seed, a.depth, a.branching, blocks=a.blocks, threads=a.threads,
+                             host_threads=a.host_threads)
+        ms = r["elapsed_ms"]
+        print(json.dumps({"workload": "uts-geo-coop", "seed": a.seed, "depth_limit": a.depth,
+                          "branching": a.branching, **r,
+                          "nodes_per_s": r["nodes"] / (ms * 1e-3) if ms > 0 else None}), flush=True)
+        return 0
     nodes, leaves, deepest, ms = uts_geo_run(a.seed, a.depth, a.branching, blocks=a.blocks, threads=a.threads)
     print(json.dumps({"workload": "uts-geo", "seed": a.seed, "depth_limit": a.depth, "branching": a.branching,
                       "nodes": nodes, "leaves": leaves, "deepest": deepest, "ms": ms,
@@ -162,6 +170,9 @@ def main(argv=None):
     ug.add_argument("--branching", type=float, default=4.0)
     ug.add_argument("--blocks", type=int, default=304)
     ug.add_argument("--threads", type=int, default=256)
+    ug.add_argument("--host-threads", type=int, default=None,
+                    help="walk cooperatively with this many host threads (-1: cores minus one; with --blocks 0 the "
+                         "host walks alone)")
     sw = sub.add_parser("sweep")
     sw.add_argument("--prims", default=SWEEP_PRIMS)
     sw.add_argument("--num-ldst", default="10")

@@ -1,6 +1,9 @@
 // hs_uts_geo.cuh -- geometric UTS walk (SHA-1 node generator, work stealing
 // over per-CTA lock-free queues); shared by the standalone kernel
-// (hs_uts_geo.cu) and the server's tree-search requests (hs_serve.cu).
+// (hs_uts_geo.cu), the cooperative CPU+GPU walk (hs_uts_geo.cu, with host
+// threads through the bridge below) and the server's tree-search requests
+// (hs_serve.cu).  The node generator is __host__ __device__: the host walkers
+// of the cooperative walk hash with the same code.
 #pragma once
 #include "../../include/hs/hs_device.cuh"
 
@@ -10,10 +13,42 @@ namespace hs {
 constexpr int kGeoMaxDepth = 30;
 constexpr int kGeoTable = 128;
 constexpr unsigned kGeoQueueCap = 512;  // items per CTA queue (power of two)
+constexpr unsigned kBridgeCap = 1024;   // items per CPU<->GPU bridge ring (power of two)
+constexpr int kHostLevels = 7;          // the GPU gives host walkers subtrees with 3..kHostLevels levels left
+constexpr int kHostMinLevels = 3;
 
 struct GeoItem {  // children [first, end) of the node with state s at `depth`
   unsigned s[5];
   unsigned depth, first, end;
+};
+
+// Cooperative walk: GPU CTAs and host threads share one tree through two
+// bounded rings in mapped pinned host memory.  Each ring has one producer side
+// and one consumer side: a side's own position word lives in its own memory
+// (the GPU's in device memory, the host's in host memory), so the rings need
+// no atomics across the link; the cells' sequence numbers carry the
+// hand-off (release/acquire at system scope).  Only the global count takes
+// system-scope atomics from both sides.
+//   ctl (host memory, one word per 128-byte line):
+//     [0]   global count: active sides (a side is active while its own count
+//           of queued items plus busy walkers is non-zero) plus items in the
+//           two rings; the walk is over when it reaches zero
+//     [32]  idle host walkers        [64]  the GPU has idle threads (host walkers give work)
+//     [96]  abort (a side timed out) [128] GPU->host ring dequeue position (host only)
+//     [160] host->GPU ring enqueue position (host only)
+//     [192] GPU heartbeat            [224] host heartbeat
+//   dev (device memory): [0] GPU->host enqueue position, [32] host->GPU
+//     dequeue position, [64] done (a poller saw the global count at zero),
+//     [96] the pollers' last view of the host (progress signature)
+static_assert(sizeof(GeoItem) == 32, "bridge cells copy items as 8 words");
+
+struct GeoBridge {
+  unsigned* ctl;
+  unsigned* g2h_seq;
+  GeoItem* g2h_item;
+  unsigned* h2g_seq;
+  GeoItem* h2g_item;
+  unsigned* dev;
 };
 
 struct GeoArgs {
@@ -28,12 +63,19 @@ struct GeoArgs {
   unsigned seed;
   unsigned* status;
   unsigned long long timeout_ns;
+  GeoBridge br;  // cooperative walk only
 };
 
-__device__ __forceinline__ unsigned rotl32(unsigned x, int n) { return __funnelshift_l(x, x, n); }
+__host__ __device__ __forceinline__ unsigned rotl32(unsigned x, int n) {
+#ifdef __CUDA_ARCH__
+  return __funnelshift_l(x, x, n);
+#else
+  return (x << n) | (x >> (32 - n));
+#endif
+}
 
 // SHA-1 (FIPS 180-4) of one padded 64-byte block given as 16 big-endian words.
-__device__ __forceinline__ void sha1_block(unsigned w[16], unsigned h[5]) {
+__host__ __device__ __forceinline__ void sha1_block(unsigned w[16], unsigned h[5]) {
   unsigned a = 0x67452301u, b = 0xEFCDAB89u, c = 0x98BADCFEu, d = 0x10325476u, e = 0xC3D2E1F0u;
 #pragma unroll
   for (int t = 0; t < 80; ++t) {
@@ -56,17 +98,18 @@ __device__ __forceinline__ void sha1_block(unsigned w[16], unsigned h[5]) {
   h[4] = 0xC3D2E1F0u + e;
 }
 
-__device__ __forceinline__ void geo_child(const unsigned p[5], unsigned i, unsigned out[5]) {
+__host__ __device__ __forceinline__ void geo_child(const unsigned p[5], unsigned i, unsigned out[5]) {
   unsigned w[16] = {p[0], p[1], p[2], p[3], p[4], i, 0x80000000u, 0, 0, 0, 0, 0, 0, 0, 0, 192u};
   sha1_block(w, out);
 }
 
-__device__ __forceinline__ void geo_root(unsigned seed, unsigned out[5]) {
+__host__ __device__ __forceinline__ void geo_root(unsigned seed, unsigned out[5]) {
   unsigned w[16] = {0, 0, 0, 0, seed, 0x80000000u, 0, 0, 0, 0, 0, 0, 0, 0, 0, 160u};
   sha1_block(w, out);
 }
 
-__device__ __forceinline__ int geo_nchildren(const unsigned s[5], int depth, int limit, const unsigned* t, int nt) {
+__host__ __device__ __forceinline__ int geo_nchildren(const unsigned s[5], int depth, int limit, const unsigned* t,
+                                                      int nt) {
   if (depth >= limit) return 0;
   const unsigned r = s[4] & 0x7fffffffu;
   int m = 0;
@@ -123,6 +166,54 @@ static __device__ bool q_pop(const GeoArgs& a, int q, GeoItem& it) {
   return false;
 }
 
+// GPU side of the bridge rings: producer of the GPU->host ring, consumer of
+// the host->GPU ring.  Items cross the link word by word at system scope.
+static __device__ bool g2h_push(const GeoBridge& br, const GeoItem& it) {
+  unsigned* enq = br.dev;
+  unsigned pos = ld_relaxed<GPU>(enq);
+  for (int tries = 0; tries < 16; ++tries) {
+    const unsigned c = pos & (kBridgeCap - 1);
+    const int dif = (int)(ld_acquire<SYS>(br.g2h_seq + c) - pos);
+    if (dif == 0) {
+      if (atomicCAS(enq, pos, pos + 1u) == pos) {
+        unsigned* dst = reinterpret_cast<unsigned*>(br.g2h_item + c);
+        const unsigned* src = reinterpret_cast<const unsigned*>(&it);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) st_relaxed<SYS>(dst + k, src[k]);
+        st_release<SYS>(br.g2h_seq + c, pos + 1u);
+        return true;
+      }
+    } else if (dif < 0) {
+      return false;  // full
+    }
+    pos = ld_relaxed<GPU>(enq);
+  }
+  return false;
+}
+
+static __device__ bool h2g_pop(const GeoBridge& br, GeoItem& it) {
+  unsigned* deq = br.dev + 32;
+  unsigned pos = ld_relaxed<GPU>(deq);
+  for (int tries = 0; tries < 16; ++tries) {
+    const unsigned c = pos & (kBridgeCap - 1);
+    const int dif = (int)(ld_acquire<SYS>(br.h2g_seq + c) - (pos + 1u));
+    if (dif == 0) {
+      if (atomicCAS(deq, pos, pos + 1u) == pos) {
+        const unsigned* src = reinterpret_cast<const unsigned*>(br.h2g_item + c);
+        unsigned* dst = reinterpret_cast<unsigned*>(&it);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) dst[k] = ld_relaxed<SYS>(src + k);
+        st_release<SYS>(br.h2g_seq + c, pos + kBridgeCap);
+        return true;
+      }
+    } else if (dif < 0) {
+      return false;  // empty
+    }
+    pos = ld_relaxed<GPU>(deq);
+  }
+  return false;
+}
+
 struct GeoFrame {
   unsigned s[5];
   int next, end;
@@ -131,9 +222,26 @@ struct GeoFrame {
 // The walk, run by every thread of the walking CTAs (rank = this CTA's index
 // among them): the standalone kernel's grid, or a server slot's CTAs.  Each
 // CTA pushes to queue rank % nq and steals from random others.
+//
+// COOP: host threads walk the same tree (hs_uts_geo.cu).  A busy thread gives
+// host walkers that are idle a subtree near the depth limit (3 to 7 levels
+// left: small, since a host core hashes some 40x slower than the GPU); idle
+// threads elect one poller per CTA at a time, at most one poll per kPollNs,
+// which takes work the host walkers gave back, asks for more once over half
+// of the grid is idle (the tail of the walk), and ends the walk for everyone
+// when the global count is zero.  The GPU side's own count (work) is then one of
+// the two sides the global count tracks.
+template <bool COOP = false>
 static __device__ void uts_geo_walk(const GeoArgs& a, unsigned rank) {
+  constexpr unsigned long long kPollNs = 16000;  // a poll costs a few link round trips
   __shared__ unsigned s_t[kGeoTable];
+  __shared__ unsigned s_poll;
+  __shared__ unsigned long long s_poll_t;
   for (int i = threadIdx.x; i < kGeoTable; i += blockDim.x) s_t[i] = i < a.nt ? a.table[i] : 0u;
+  if (threadIdx.x == 0) {
+    s_poll = 0u;
+    s_poll_t = 0ull;
+  }
   __syncthreads();
   const HsEnv env{a.status, a.timeout_ns};
   const int myq = (int)(rank % (unsigned)a.nq);
@@ -144,6 +252,7 @@ static __device__ void uts_geo_walk(const GeoArgs& a, unsigned rank) {
   unsigned long long nodes = 0, leaves = 0;
   unsigned deepest = 0;
   bool busy = false;
+  unsigned batches = 0;
   if (rank == 0 && threadIdx.x == 0) {  // the root; work starts at 1 for this thread
     unsigned r[5];
     geo_root(a.seed, r);
@@ -151,7 +260,11 @@ static __device__ void uts_geo_walk(const GeoArgs& a, unsigned rank) {
     const int m = geo_nchildren(r, 0, a.limit, s_t, a.nt);
     if (m == 0) {
       leaves = 1;
-      asm volatile("red.release.gpu.global.add.u32 [%0], %1;" :: "l"(a.work), "r"(0xFFFFFFFFu) : "memory");
+      if constexpr (COOP) {
+        if (atom_add_acqrel<GPU>(a.work, 0xFFFFFFFFu) == 1u) atom_add_acqrel<SYS>(a.br.ctl, 0xFFFFFFFFu);
+      } else {
+        asm volatile("red.release.gpu.global.add.u32 [%0], %1;" :: "l"(a.work), "r"(0xFFFFFFFFu) : "memory");
+      }
     } else {
       for (int k = 0; k < 5; ++k) st[0].s[k] = r[k];
       st[0].next = 0;
@@ -193,8 +306,35 @@ static __device__ void uts_geo_walk(const GeoArgs& a, unsigned rank) {
       }
       if (sp == 0) {
         busy = false;
-        asm volatile("red.release.gpu.global.add.u32 [%0], %1;" :: "l"(a.work), "r"(0xFFFFFFFFu) : "memory");
+        if constexpr (COOP) {
+          if (atom_add_acqrel<GPU>(a.work, 0xFFFFFFFFu) == 1u) atom_add_acqrel<SYS>(a.br.ctl, 0xFFFFFFFFu);
+        } else {
+          asm volatile("red.release.gpu.global.add.u32 [%0], %1;" :: "l"(a.work), "r"(0xFFFFFFFFu) : "memory");
+        }
         continue;
+      }
+      if constexpr (COOP) {
+        if ((++batches & 15u) == 0u) {  // every 1024 nodes: heartbeat, and feed idle host walkers
+          if (threadIdx.x == 0) st_relaxed<SYS>(a.br.ctl + 192, (unsigned)(globaltimer() >> 16));
+          const unsigned hidle = ld_relaxed<SYS>(a.br.ctl + 32);
+          if (hidle != 0u && ld_relaxed<GPU>(a.br.dev) - ld_relaxed<SYS>(a.br.ctl + 128) < hidle) {
+            for (int f = 0; f < sp; ++f) {
+              const int left = st[f].end - st[f].next;
+              const int levels = a.limit - (int)(base + (unsigned)f);
+              if (left >= 2 && levels <= kHostLevels && levels >= kHostMinLevels) {
+                GeoItem it;
+                for (int k = 0; k < 5; ++k) it.s[k] = st[f].s[k];
+                it.depth = base + (unsigned)f;
+                it.first = (unsigned)(st[f].next + left / 2);
+                it.end = (unsigned)st[f].end;
+                atom_add_acqrel<SYS>(a.br.ctl, 1u);
+                if (g2h_push(a.br, it)) st[f].end = (int)it.first;
+                else atom_add_acqrel<SYS>(a.br.ctl, 0xFFFFFFFFu);
+                break;
+              }
+            }
+          }
+        }
       }
       if (ld_relaxed<GPU>(a.idle) != 0u) {
         // give away the upper half of the oldest frame with two or more children left
@@ -222,6 +362,34 @@ static __device__ void uts_geo_walk(const GeoArgs& a, unsigned rank) {
       rng ^= rng << 13; rng ^= rng >> 17; rng ^= rng << 5;
       got = q_pop(a, (int)(rng % (unsigned)a.nq), it);
     }
+    unsigned w = 0;
+    if constexpr (COOP) {
+      if (!got && ld_relaxed<GPU>(a.br.dev + 64) != 0u) break;  // done
+      const unsigned long long now = globaltimer();
+      if (!got && now - *(volatile unsigned long long*)&s_poll_t >= kPollNs && atomicCAS(&s_poll, 0u, 1u) == 0u) {
+        s_poll_t = now;
+        if (h2g_pop(a.br, it)) {
+          got = true;
+          // the item's share of the global count becomes this side's, unless the side was active already
+          if (atom_add_acqrel<GPU>(a.work, 1u) != 0u) atom_add_acqrel<SYS>(a.br.ctl, 0xFFFFFFFFu);
+        } else {
+          const unsigned g = ld_acquire<SYS>(a.br.ctl);
+          const unsigned ab = ld_relaxed<SYS>(a.br.ctl + 96);
+          if (g == 0u || ab != 0u) {
+            if (ab != 0u) fail(env, HS_DEV_TIMEOUT, HS_SITE_UTS);
+            st_release<GPU>(a.br.dev + 64, 1u);
+            atomicExch(&s_poll, 0u);
+            break;
+          }
+          // ask the host walkers for work once more than half of this side's threads are idle
+          if (ld_relaxed<GPU>(a.work) < gridDim.x * blockDim.x / 2u && ld_relaxed<SYS>(a.br.ctl + 64) == 0u)
+            st_relaxed<SYS>(a.br.ctl + 64, 1u);
+          st_relaxed<GPU>(a.br.dev + 96, g * 0x9E3779B1u ^ ld_relaxed<SYS>(a.br.ctl + 224));
+        }
+        atomicExch(&s_poll, 0u);
+      }
+      if (!got) w = ld_acquire<GPU>(a.work) ^ (ld_relaxed<GPU>(a.br.dev + 96) * 0x85EBCA77u);
+    }
     if (got) {
       if (counted_idle) {
         atomicSub(a.idle, 1u);
@@ -241,15 +409,21 @@ static __device__ void uts_geo_walk(const GeoArgs& a, unsigned rank) {
       atomicAdd(a.idle, 1u);
       counted_idle = true;
     }
-    const unsigned w = ld_acquire<GPU>(a.work);
-    if (w == 0u) break;
-    // bounded: the work count must move within the time limit
+    if constexpr (!COOP) {
+      w = ld_acquire<GPU>(a.work);
+      if (w == 0u) break;
+    }
+    // bounded: the work count (and, cooperative, the host's view) must move within the time limit
     const unsigned long long now = globaltimer();
     if (t0 == 0 || w != last_work) {
       t0 = now;
       last_work = w;
     } else if (now - t0 > a.timeout_ns || ld_relaxed<GPU>(a.status) != 0u) {
       if (ld_relaxed<GPU>(a.status) == 0u) fail(env, HS_DEV_TIMEOUT, HS_SITE_UTS);
+      if constexpr (COOP) {
+        st_relaxed<SYS>(a.br.ctl + 96, 1u);  // the host walkers stop too
+        st_release<GPU>(a.br.dev + 64, 1u);
+      }
       break;
     }
     sleep_ns(nap);

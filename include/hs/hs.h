@@ -267,6 +267,29 @@ int hs_uts_geo_table(double branching, uint32_t* table, int n);
 int hs_uts_geo_run(unsigned seed, int depth_limit, double branching, int blocks, int threads,
                    unsigned long long timeout_ns, hs_uts_geo_result* r);
 
+/* Cooperative CPU+GPU walk of the same tree: `blocks` CTAs and `host_threads`
+ * host threads balance load dynamically through two rings in mapped pinned
+ * host memory (README.txt:30 of the reference names CPU+GPU load balancing for
+ * UTS; its uts.cu:457-539 host threads do no tree work).  The GPU gives idle
+ * host walkers subtrees with 3 to 7 levels left; host walkers give the GPU
+ * the upper half of their oldest frame once over half of its threads idle.
+ * host_threads < 0: the host's cores minus one.  blocks == 0: host threads
+ * only, with no CUDA call (the walk runs on a machine without a GPU).  GPU and
+ * host threads together need a link with native host atomics
+ * (cudaDevAttrHostNativeAtomicSupported, NVLink-C2C); HS_EINVAL otherwise.
+ * Waits are bounded on both sides: no progress for timeout_ns → HS_ETIMEDOUT. */
+typedef struct hs_uts_coop_result {
+  unsigned long long nodes, leaves;
+  unsigned max_depth;
+  unsigned long long gpu_nodes, host_nodes; /* nodes each side expanded */
+  unsigned long long to_host, to_gpu;       /* items that crossed the link each way */
+  int host_threads;                         /* walkers that ran */
+  float elapsed_ms;                         /* wall time, launch to both sides done */
+  unsigned dev_error_bits;
+} hs_uts_coop_result;
+int hs_uts_geo_coop_run(unsigned seed, int depth_limit, double branching, int blocks, int threads, int host_threads,
+                        unsigned long long timeout_ns, hs_uts_coop_result* r);
+
 /* ---- tree barrier with local exchange on thread-block clusters ----------------- */
 /* The LocalExch tree barriers (main.cu:153-270; joinBarrier_helper,
  * cudaLocksBarrierAtomic.cu:147-172; joinLFBarrier_helper,

@@ -55,12 +55,13 @@ constexpr int kLineWords = 32;
 // ---------------------------------------------------------------------------
 // Scoped memory operations (generic addressing: global or distributed shared).
 // ---------------------------------------------------------------------------
-enum Scope { GPU = 0, CLUSTER = 1, CTA = 2 };
+enum Scope { GPU = 0, CLUSTER = 1, CTA = 2, SYS = 3 };  // SYS: host memory shared with CPU threads
 
 template <int S> __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   unsigned v;
   if constexpr (S == CLUSTER) asm volatile("ld.acquire.cluster.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   else if constexpr (S == CTA) asm volatile("ld.acquire.cta.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  else if constexpr (S == SYS) asm volatile("ld.acquire.sys.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   else asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
@@ -68,17 +69,20 @@ template <int S> __device__ __forceinline__ unsigned ld_relaxed(const unsigned* 
   unsigned v;
   if constexpr (S == CLUSTER) asm volatile("ld.relaxed.cluster.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   else if constexpr (S == CTA) asm volatile("ld.relaxed.cta.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  else if constexpr (S == SYS) asm volatile("ld.relaxed.sys.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   else asm volatile("ld.relaxed.gpu.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
 template <int S> __device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
   if constexpr (S == CLUSTER) asm volatile("st.release.cluster.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
   else if constexpr (S == CTA) asm volatile("st.release.cta.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+  else if constexpr (S == SYS) asm volatile("st.release.sys.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
   else asm volatile("st.release.gpu.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
 }
 template <int S> __device__ __forceinline__ void st_relaxed(unsigned* p, unsigned v) {
   if constexpr (S == CLUSTER) asm volatile("st.relaxed.cluster.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
   else if constexpr (S == CTA) asm volatile("st.relaxed.cta.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+  else if constexpr (S == SYS) asm volatile("st.relaxed.sys.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
   else asm volatile("st.relaxed.gpu.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
 }
 // atom.inc: old = *p; *p = (old >= lim) ? 0 : old + 1   (same wrap rule as atomicInc)
@@ -99,6 +103,7 @@ template <int S> __device__ __forceinline__ void red_release_add(unsigned* p, un
 template <int S> __device__ __forceinline__ unsigned atom_add_acqrel(unsigned* p, unsigned v) {
   unsigned o;
   if constexpr (S == CLUSTER) asm volatile("atom.acq_rel.cluster.add.u32 %0, [%1], %2;" : "=r"(o) : "l"(p), "r"(v) : "memory");
+  else if constexpr (S == SYS) asm volatile("atom.acq_rel.sys.add.u32 %0, [%1], %2;" : "=r"(o) : "l"(p), "r"(v) : "memory");
   else asm volatile("atom.acq_rel.gpu.add.u32 %0, [%1], %2;" : "=r"(o) : "l"(p), "r"(v) : "memory");
   return o;
 }
