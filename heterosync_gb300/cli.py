@@ -16,9 +16,10 @@
       geometric SHA-1 UTS by work stealing; node, leaf and depth counts
 
   python -m heterosync_gb300.cli sweep [--prims "..."] [--num-ldst 10]
-         [--num-tbs ...] [--iters 10] [--runs 1]
+         [--num-tbs ...] [--iters 10] [--runs 1] [--graph]
       the results-script sweep through the drop-in program; one JSON line per
       (primitive, numLdSt, numTBs) with the parsed `average` durations
+      (--graph: each point in this process, its repeats one CUDA graph)
 
   python -m heterosync_gb300.cli batch [--seed 20260101] [--n 64]
          [--iter-div 1] [--tune-div 25] [--plan cl,se,v,stage,bo]
@@ -124,6 +125,14 @@ def cmd_sweep(a):
         for L in (int(x) for x in a.num_ldst.split(",")):
             for G in tbs:
                 durations = []
+                if a.graph:
+                    point_ok, durations = _graph_point(prim, L, G, a.iters, a.runs)
+                    ok = ok and point_ok
+                    vals = [d for d in durations if d is not None]
+                    print(json.dumps({"syncPrim": prim, "numLdSt": L, "numTBs": G, "numCSIters": a.iters,
+                                      "durations_ms": durations, "graph": True, "bit_exact": point_ok,
+                                      "average_ms": sum(vals) / len(vals) if vals else None}), flush=True)
+                    continue
                 for _ in range(a.runs):
                     p = subprocess.run([exe, prim, str(L), str(G), str(a.iters)], capture_output=True, text=True)
                     line = next((x for x in p.stdout.splitlines() if "average" in x), "")
@@ -137,6 +146,34 @@ def cmd_sweep(a):
                                   "durations_ms": durations,
                                   "average_ms": sum(vals) / len(vals) if vals else None}), flush=True)
     return 0 if ok else 1
+
+
+def _graph_point(prim, num_ldst, num_tbs, iters, runs):
+    """One sweep point in this process: the program's run (32 threads, 10
+    repeats, the reference critical section) with the repeats replayed as one
+    CUDA graph; each run's final storage checked against the golden's closed
+    form.  Returns (all runs exact, per-run average launch ms)."""
+    import numpy as np
+    from . import RUN_GRAPH, HsError, RunConfig, expected_storage, run, storage_words
+    cfg = RunConfig(prim, num_ldst, num_tbs, iters, threads=32, repeats=10, mode="ref", flags=RUN_GRAPH)
+    try:
+        words = storage_words(cfg)
+    except HsError:
+        return False, [None] * runs
+    init = np.random.default_rng(20260101).integers(0, 1000, size=words).astype(np.uint32)
+    want = expected_storage(cfg, init)
+    ok, durations = True, []
+    for _ in range(runs):
+        st = init.copy()
+        try:
+            r = run(cfg, st)
+        except HsError:
+            ok = False
+            durations.append(None)
+            continue
+        ok = ok and bool(np.array_equal(st, want))
+        durations.append(r.avg_ms)
+    return ok, durations
 
 
 def cmd_serve(a):
@@ -179,6 +216,8 @@ def main(argv=None):
     sw.add_argument("--num-tbs", default="", help="comma list; default 1, 2, 4, 8 TBs per SM")
     sw.add_argument("--iters", type=int, default=10)
     sw.add_argument("--runs", type=int, default=1)
+    sw.add_argument("--graph", action="store_true",
+                    help="run each point in this process with its repeats replayed as one CUDA graph")
     sv = sub.add_parser("serve")
     sv.add_argument("--seed", type=int, default=20260101)
     sv.add_argument("--n", type=int, default=256)

@@ -347,6 +347,10 @@ struct hs_ctx {
   void* staging = nullptr;
   size_t staging_cap = 0;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // HS_RUN_GRAPH: the last captured repeats and what they were captured for
+  cudaStream_t gstream = nullptr;  // capture stream when the caller passes the legacy default stream
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<unsigned char> gkey;
 };
 
 static int ensure(void** p, size_t* cap, size_t bytes) {
@@ -393,6 +397,8 @@ extern "C" int hs_ctx_destroy(hs_ctx* c) {
   cudaFree(c->staging);
   for (auto& ev : c->ev)
     if (ev) cudaEventDestroy(ev);
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->gstream) cudaStreamDestroy(c->gstream);
   delete c;
   return HS_OK;
 }
@@ -494,6 +500,10 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c0, void* storage, int o
   int s = validate(c, nsm);
   if (s) return r->status = s;
   if (c->threads > ctx->max_tpb) { g_err = "threads per TB above the device limit"; return r->status = HS_EINVAL; }
+  if ((c->flags & HS_RUN_GRAPH) && (c->flags & HS_RUN_SYNC_EACH)) {
+    g_err = "HS_RUN_GRAPH replays the repeats as one graph: no host synchronisation between them";
+    return r->status = HS_EINVAL;
+  }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   HS_CK(cudaSetDevice(ctx->device));
   size_t words = 0;
@@ -597,18 +607,64 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c0, void* storage, int o
   lc.stream = st;
   lc.attrs = attr;
   lc.numAttrs = cluster > 1 ? 1 : 0;
-  HS_CK(cudaEventRecord(ctx->ev[0], st));
-  for (int rep = 0; rep < c->repeats; ++rep) {
-    void* args[] = {&d};
-    HS_CK(cudaLaunchKernelExC(&lc, (const void*)fn, args));
-    r->launches++;
-    if (c->flags & HS_RUN_SYNC_EACH) HS_CK(cudaStreamSynchronize(st));
+  cudaStream_t lst = st;  // the stream the repeats run on
+  if ((c->flags & HS_RUN_GRAPH) && c->repeats > 0) {
+    // A capture cannot run on the legacy default stream: use a blocking stream
+    // of the context, which orders itself with the legacy stream's work.
+    if (!st) {
+      if (!ctx->gstream) HS_CK(cudaStreamCreate(&ctx->gstream));
+      lst = ctx->gstream;
+    }
+    std::vector<unsigned char> key(sizeof(RunDesc) + sizeof(lc.gridDim) + sizeof(lc.blockDim) + 4 * sizeof(size_t));
+    size_t o = 0;
+    auto put = [&](const void* p, size_t n) { std::memcpy(key.data() + o, p, n); o += n; };
+    const size_t extra[4] = {(size_t)fn, smem, (size_t)cluster, (size_t)c->repeats};
+    put(&d, sizeof(RunDesc));
+    put(&lc.gridDim, sizeof(lc.gridDim));
+    put(&lc.blockDim, sizeof(lc.blockDim));
+    put(extra, sizeof(extra));
+    if (!ctx->gexec || key != ctx->gkey) {
+      if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+      ctx->gexec = nullptr;
+      ctx->gkey.clear();
+      HS_CK(cudaStreamBeginCapture(lst, cudaStreamCaptureModeThreadLocal));
+      lc.stream = lst;
+      cudaError_t ce = cudaSuccess;
+      for (int rep = 0; rep < c->repeats && ce == cudaSuccess; ++rep) {
+        void* args[] = {&d};
+        ce = cudaLaunchKernelExC(&lc, (const void*)fn, args);
+      }
+      cudaGraph_t g = nullptr;
+      const cudaError_t ee = cudaStreamEndCapture(lst, &g);
+      if (ce == cudaSuccess && ee == cudaSuccess) ce = cudaGraphInstantiate(&ctx->gexec, g, 0);
+      if (g) cudaGraphDestroy(g);
+      if (ce != cudaSuccess || ee != cudaSuccess) {
+        cudaGetLastError();
+        ctx->gexec = nullptr;
+        g_err = std::string("graph capture: ") + cudaGetErrorString(ce != cudaSuccess ? ce : ee);
+        return r->status = HS_ECUDA;
+      }
+      ctx->gkey = key;
+    }
+    HS_CK(cudaEventRecord(ctx->ev[0], lst));
+    HS_CK(cudaGraphLaunch(ctx->gexec, lst));
+    r->launches += (unsigned)c->repeats;
+    HS_CK(cudaEventRecord(ctx->ev[1], lst));
+  } else {
+    HS_CK(cudaEventRecord(ctx->ev[0], st));
+    for (int rep = 0; rep < c->repeats; ++rep) {
+      void* args[] = {&d};
+      HS_CK(cudaLaunchKernelExC(&lc, (const void*)fn, args));
+      r->launches++;
+      if (c->flags & HS_RUN_SYNC_EACH) HS_CK(cudaStreamSynchronize(st));
+    }
+    HS_CK(cudaEventRecord(ctx->ev[1], st));
   }
-  HS_CK(cudaEventRecord(ctx->ev[1], st));
   hs_note_launches(r->launches);
   if (!on_device) {
     HS_CK(cudaMemcpyAsync(storage, dev, bytes, cudaMemcpyDeviceToHost, st));
   }
+  if (lst != st) HS_CK(cudaStreamSynchronize(lst));
   HS_CK(cudaStreamSynchronize(st));
   HS_CK(cudaEventElapsedTime(&r->elapsed_ms, ctx->ev[0], ctx->ev[1]));
   if (!on_device) HS_CK(cudaEventElapsedTime(&r->h2d_ms, ctx->ev[2], ctx->ev[3]));

@@ -47,7 +47,9 @@ enum {
   HS_RUN_SYNC_EACH = 1,   /* host-synchronise after every launch, as main.cu:844-854 does */
   HS_RUN_KEEP_STATE = 2,  /* do not re-initialise lock state before the repeats */
   HS_RUN_NO_CLUSTER = 4,  /* tree barriers: keep the local stage in L2 instead of on thread-block clusters */
-  HS_RUN_REGISTER_CS = 8  /* critical sections on the register path only (no bulk copies through shared memory) */
+  HS_RUN_REGISTER_CS = 8, /* critical sections on the register path only (no bulk copies through shared memory) */
+  HS_RUN_GRAPH = 16       /* the repeats as one CUDA graph: captured once per context and launch shape, then
+                             replayed (not with HS_RUN_SYNC_EACH); the lock state is still reset before it */
 };
 
 /* One run of one SyncPrims primitive: `repeats` launches of `num_tbs` TBs of
