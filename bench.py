@@ -217,6 +217,40 @@ def l2_atomic_peak(hs):
     return v.value, same.value
 
 
+# The lock kernels' latency floor per op, from the measured hand-off latencies:
+# a CAS lock's next holder sees the release (one hand-off), wins its atomic,
+# loads its critical section and waits for its stores' ack before releasing;
+# a queue lock (ticket, ring slot) takes its place in advance, so no atomic
+# sits on the chain.
+LOCK_CHAIN = {"spinMutex": "cas", "spinMutexEBO": "cas", "faMutex": "queue", "sleepMutex": "queue",
+              "spinSem1": "cas", "spinSem2": "cas", "spinSem10": "cas", "spinSem120": "cas",
+              "spinSemEBO1": "cas", "spinSemEBO2": "cas", "spinSemEBO10": "cas", "spinSemEBO120": "cas"}
+
+
+def lock_latency(hs, recs, nsm):
+    """Per-op latency floor of each lock cell at numTBs = NUM_SM, numLdSt 10
+    (where every semaphore TB is a writer and the op is a pure hand-off),
+    against the measured time per op."""
+    lat = hs.probe_latency(256)
+    h, a, ld = lat["handoff_ns_median"], lat["atomic_rtt_ns"], lat["load_rtt_ns"]
+    floor = {"cas": h + a + 2 * ld, "queue": h + 2 * ld}
+    cells = {}
+    for r in recs:
+        if r["prim"] in LOCK_CHAIN and r["num_tbs"] == nsm and r["num_ldst"] == 10:
+            us = r["ms"] * 1e3 / r["ops"]
+            f = floor[LOCK_CHAIN[r["prim"]]] * 1e-3
+            cells.setdefault(r["prim"], []).append((us, f))
+    return {"handoff_ns": {"median": h, "min": lat["handoff_ns_min"], "max": lat["handoff_ns_max"],
+                           "partners": lat["partners"]},
+            "atomic_rtt_ns": a, "load_rtt_ns": ld,
+            "floor_ns": {"cas_lock": floor["cas"], "queue_lock": floor["queue"]},
+            "model": "cas lock: hand-off + atomic + CS load + store ack (2 x L2 load); queue lock: no atomic",
+            "cells_152x10": {k: {"us_per_op": round(sum(u for u, _ in v) / len(v), 3),
+                                 "floor_us": round(v[0][1], 3),
+                                 "frac": round(v[0][1] / (sum(u for u, _ in v) / len(v)), 3)}
+                             for k, v in cells.items()}}
+
+
 # algorithmic L2 atomics per sync op (contention-free minimum of this build's
 # implementation of each primitive): lock + unlock
 ATOMICS_PER_OP = {"spinMutex": 2, "spinMutexEBO": 2, "sleepMutex": 3, "faMutex": 2,
@@ -544,6 +578,10 @@ def main():
         dd = by_prim[dom]
         achieved = dd["bytes"] / (dd["ms"] * 1e-3) / 1e9
         atom_peak, same_rate = l2_atomic_peak(hs)
+        try:
+            lock_latency_out = lock_latency(hs, recs, nsm)
+        except Exception as e:  # noqa: BLE001
+            lock_latency_out = {"error": str(e)}
         atom_achieved = sum(by_prim[k]["ops"] * ATOMICS_PER_OP[k] for k in by_prim) / dev_s
         sub = [r for r in recs if r["prim"] in REF_PRIMS]
         sub_ops = sum(r["ops"] for r in sub)
@@ -576,6 +614,7 @@ def main():
                           "frac": (atom_achieved / atom_peak) if atom_peak else None, "unit": "atomics/s",
                           "same_address_rate": same_rate,
                           "note": "peak: contention-free red.add probe; same_address_rate: one word"},
+            "lock_latency": lock_latency_out,
             "same_subset": same_subset,
             "per_prim": {k: {"ops_per_s": v["ops"] / (v["ms"] * 1e-3), "ms": round(v["ms"], 3)}
                          for k, v in by_prim.items()},

@@ -453,6 +453,24 @@ def uts_geo_run(seed: int, depth_limit: int, branching: float = 4.0, blocks: int
     return r.nodes, r.leaves, r.max_depth, r.elapsed_ms
 
 
+class _LatencyResult(ctypes.Structure):
+    _fields_ = [("handoff_ns_median", ctypes.c_double), ("handoff_ns_min", ctypes.c_double),
+                ("handoff_ns_max", ctypes.c_double), ("atomic_rtt_ns", ctypes.c_double),
+                ("load_rtt_ns", ctypes.c_double), ("partners", ctypes.c_int), ("dev_error_bits", ctypes.c_uint)]
+
+
+def probe_latency(rounds: int = 256) -> dict:
+    """Lock hand-off latencies on this GPU (hs_probe_latency): flag ping-pong
+    between SMs (one hand-off = half a round trip; median, min, max over the
+    SMs), dependent L2 atomics and dependent L2 loads, in ns."""
+    r = _LatencyResult()
+    lib().hs_probe_latency.argtypes = [ctypes.c_int, ctypes.c_void_p]
+    s = lib().hs_probe_latency(rounds, ctypes.byref(r))
+    if s:
+        raise HsError(s, "hs_probe_latency failed")
+    return {f: getattr(r, f) for f, _ in _LatencyResult._fields_}
+
+
 class _CoopResult(ctypes.Structure):
     _fields_ = [("nodes", ctypes.c_ulonglong), ("leaves", ctypes.c_ulonglong), ("max_depth", ctypes.c_uint),
                 ("gpu_nodes", ctypes.c_ulonglong), ("host_nodes", ctypes.c_ulonglong),

@@ -1,12 +1,23 @@
 // hs_probe.cu -- roofline probes measured on the local GPU.
 //
+// Lock hand-off latencies (hs_probe_latency): the floor under a serialised
+// lock's op is a chain of such latencies (the release seen by the next
+// holder, its atomic, its critical section's load and the store ack before
+// its own release), so these set the sync-ops bound for the lock kernels.
+//
 // L2 atomic rate: every thread issues red.relaxed.gpu.global.add.u32 to its own
 // word, words 128 bytes apart, so no two atomics contend for a line: the
 // aggregate rate is the chip's contention-free L2 atomic throughput, the
 // denominator of the sync-ops roofline.
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cstdint>
+#include <cstring>
+#include <numeric>
+#include <random>
+#include <vector>
 #include "../../include/hs/hs.h"
+#include "../../include/hs/hs_device.cuh"
 
 namespace hs {
 
@@ -23,9 +34,130 @@ __global__ void k_probe_same(unsigned* word, int iters) {
     for (int i = 0; i < iters; ++i) asm volatile("red.relaxed.gpu.global.add.u32 [%0], 1;" :: "l"(word) : "memory");
 }
 
+constexpr unsigned long long kLatTimeoutNs = 2000000000ull;
+
+// Bounded poll until *f == want; false (and err set) on timeout or another side's error.
+__device__ bool lat_wait(const unsigned* f, unsigned want, unsigned* err, unsigned long long t_start) {
+  for (unsigned spin = 0;; ++spin) {
+    if (ld_acquire<GPU>(f) == want) return true;
+    if ((spin & 255u) == 255u) {
+      if (ld_relaxed<GPU>(err) != 0u) return false;
+      if (globaltimer() - t_start > kLatTimeoutNs) {
+        atomicOr(err, 1u);
+        return false;
+      }
+    }
+  }
+}
+
+// One thread per CTA works; grid = one CTA per SM (cooperative launch: all co-resident).
+__global__ void k_probe_latency(unsigned* flags, unsigned long long* ns, unsigned* chase, unsigned* lines,
+                                int rounds, int chain, unsigned zmask, unsigned* err) {
+  if (threadIdx.x != 0) return;
+  const unsigned long long t_start = globaltimer();
+  const unsigned k = blockIdx.x;
+  if (k != 0) {  // partner k: answer CTA 0's rounds when its turn comes
+    unsigned* f = flags + (size_t)k * 32;
+    for (int i = 0; i < rounds; ++i) {
+      if (!lat_wait(f, 2u * i + 1u, err, t_start)) return;
+      st_release<GPU>(f, 2u * i + 2u);
+    }
+    return;
+  }
+  for (unsigned p = 1; p < gridDim.x; ++p) {
+    unsigned* f = flags + (size_t)p * 32;
+    const unsigned long long t0 = globaltimer();
+    for (int i = 0; i < rounds; ++i) {
+      st_release<GPU>(f, 2u * i + 1u);
+      if (!lat_wait(f, 2u * i + 2u, err, t_start)) return;
+    }
+    ns[p] = globaltimer() - t0;
+  }
+  // dependent atomics: the next line's index depends on the returned value
+  // (zmask is 0 at run time, unknown to the compiler)
+  unsigned z = 0;
+  unsigned long long t0 = globaltimer();
+  for (int i = 0; i < chain; ++i) {
+    unsigned old;
+    asm volatile("atom.relaxed.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(lines + (size_t)((i * 37) & 63) * 32 + z) : "memory");
+    z = old & zmask;
+  }
+  ns[gridDim.x] = globaltimer() - t0;
+  // dependent L2 loads around the linked cycle
+  unsigned idx = 0;
+  t0 = globaltimer();
+  for (int i = 0; i < chain; ++i) idx = ld_relaxed<GPU>(chase + idx);
+  ns[gridDim.x + 1] = globaltimer() - t0;
+  ns[gridDim.x + 2] = idx;  // keeps the chain live
+}
+
 }  // namespace hs
 
 void hs_note_launches(unsigned n);
+
+extern "C" int hs_probe_latency(int rounds, hs_latency_result* r) {
+  if (rounds <= 0 || rounds > (1 << 20) || !r) return HS_EINVAL;
+  std::memset(r, 0, sizeof(*r));
+  int dev = 0, nsm = 0, coop = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop || nsm < 2) {
+    cudaGetLastError();
+    return HS_ENODEV;
+  }
+  constexpr unsigned kCycle = 4096;  // 128-byte lines: 512 KiB, L2-resident
+  const int chain = 4096;
+  std::vector<unsigned> cyc(kCycle * 32, 0u), order(kCycle);
+  std::iota(order.begin(), order.end(), 0u);
+  std::shuffle(order.begin() + 1, order.end(), std::mt19937(12345));
+  for (unsigned i = 0; i < kCycle; ++i) cyc[order[i] * 32] = order[(i + 1) % kCycle] * 32;
+  unsigned *flags = nullptr, *chase = nullptr, *lines = nullptr, *err = nullptr;
+  unsigned long long* ns = nullptr;
+  if (cudaMalloc(&flags, (size_t)nsm * 32 * 4) != cudaSuccess || cudaMalloc(&chase, cyc.size() * 4) != cudaSuccess ||
+      cudaMalloc(&lines, 64 * 32 * 4) != cudaSuccess || cudaMalloc(&err, 4) != cudaSuccess ||
+      cudaMalloc(&ns, (size_t)(nsm + 3) * 8) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(flags); cudaFree(chase); cudaFree(lines); cudaFree(err); cudaFree(ns);
+    return HS_ENORES;
+  }
+  cudaMemcpy(chase, cyc.data(), cyc.size() * 4, cudaMemcpyHostToDevice);
+  cudaMemset(lines, 0, 64 * 32 * 4);
+  cudaError_t e = cudaSuccess;
+  std::vector<unsigned long long> h(nsm + 3, 0ull);
+  unsigned herr = 0;
+  for (int pass = 0; pass < 2 && e == cudaSuccess && herr == 0; ++pass) {  // pass 0 warms lines and code
+    cudaMemset(flags, 0, (size_t)nsm * 32 * 4);
+    cudaMemset(err, 0, 4);
+    cudaMemset(ns, 0, (size_t)(nsm + 3) * 8);
+    int rr = pass ? rounds : 8, ch = pass ? chain : (int)kCycle;
+    unsigned zmask = 0;
+    void* args[] = {&flags, &ns, &chase, &lines, &rr, &ch, &zmask, &err};
+    e = cudaLaunchCooperativeKernel((const void*)hs::k_probe_latency, dim3((unsigned)nsm), dim3(32), args, 0, 0);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    hs_note_launches(1);
+    if (e == cudaSuccess) {
+      cudaMemcpy(&herr, err, 4, cudaMemcpyDeviceToHost);
+      cudaMemcpy(h.data(), ns, h.size() * 8, cudaMemcpyDeviceToHost);
+    }
+  }
+  cudaFree(flags); cudaFree(chase); cudaFree(lines); cudaFree(err); cudaFree(ns);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return HS_ECUDA;
+  }
+  r->dev_error_bits = herr;
+  if (herr) return HS_ETIMEDOUT;
+  std::vector<double> ho;
+  for (int p = 1; p < nsm; ++p) ho.push_back((double)h[p] / (2.0 * rounds));
+  std::sort(ho.begin(), ho.end());
+  r->partners = (int)ho.size();
+  r->handoff_ns_min = ho.front();
+  r->handoff_ns_max = ho.back();
+  r->handoff_ns_median = ho[ho.size() / 2];
+  r->atomic_rtt_ns = (double)h[nsm] / chain;
+  r->load_rtt_ns = (double)h[nsm + 1] / chain;
+  return HS_OK;
+}
 
 extern "C" int hs_probe_l2_atomics(int blocks, int threads, int iters, int same_address, double* atomics_per_s) {
   if (blocks <= 0 || threads <= 0 || threads > 1024 || iters <= 0 || !atomics_per_s) return HS_EINVAL;

@@ -373,6 +373,23 @@ int hs_serve_drive(hs_server* s, const hs_serve_request* reqs, int n, const uint
  * contended lock word sustains).  Result in atomics per second. */
 int hs_probe_l2_atomics(int blocks, int threads, int iters, int same_address, double* atomics_per_s);
 
+/* The latencies a lock hand-off is made of, each measured by one thread:
+ *  handoff: CTA 0 and each other CTA (one per SM, cooperative launch) ping-pong
+ *           a flag `rounds` times (st.release.gpu, then ld.acquire.gpu polls until
+ *           the answer shows); one hand-off = half a round trip.  Median, min and
+ *           max over the partners (SMs on both dies).
+ *  atomic:  a dependent chain of atom.add.gpu over 64 lines spread across L2.
+ *  load:    a dependent chain of ld.relaxed.gpu (L2 hits, L1 bypassed) over a
+ *           randomly linked 512 KiB cycle of 128-byte lines.
+ * Waits are bounded (2 s); a timeout sets dev_error_bits and returns HS_ETIMEDOUT. */
+typedef struct hs_latency_result {
+  double handoff_ns_median, handoff_ns_min, handoff_ns_max;
+  double atomic_rtt_ns, load_rtt_ns;
+  int partners;
+  unsigned dev_error_bits;
+} hs_latency_result;
+int hs_probe_latency(int rounds, hs_latency_result* r);
+
 /* ---- the reference's host API (cuda/syncPrims/uvm/cudaLocks.h:4-26) ----------- */
 /* Same field order as cudaLockData_t (cudaLocks.h:4-16). */
 typedef struct hs_lock_data {
