@@ -33,6 +33,7 @@ CU_SOURCES = [
     "hs_syncprims.cu",
     "hs_api.cu",
     "hs_probe.cu",
+    "hs_cohort.cu",
     "hs_noalloc.cu",
     "hs_relaxed.cu",
     "hs_relaxed_api.cu",

@@ -351,7 +351,34 @@ struct hs_ctx {
   cudaStream_t gstream = nullptr;  // capture stream when the caller passes the legacy default stream
   cudaGraphExec_t gexec = nullptr;
   std::vector<unsigned char> gkey;
+  // cohort mutexes: die map and per-die lock lines (hs_cohort.cu); state 0 not
+  // yet calibrated, 1 ready, -1 unavailable on this part
+  unsigned* coh_pool = nullptr;
+  int coh_state = 0;
+  unsigned* coh_lines[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 };
+
+// The cohort pool, calibrated on first use; false if the part has no two-die split.
+static bool cohort_ready(hs_ctx* ctx) {
+  if (ctx->coh_state == 0) {
+    ctx->coh_state = -1;
+    const size_t words = kCohortMapWords + (size_t)kCohortCandidates * kLineWords;
+    if (cudaMalloc(&ctx->coh_pool, words * 4) != cudaSuccess) {
+      cudaGetLastError();
+      ctx->coh_pool = nullptr;
+      return false;
+    }
+    cudaMemset(ctx->coh_pool, 0, words * 4);
+    int sel[2][3];
+    if (hs_cohort_calibrate(ctx->device, ctx->coh_pool, kCohortCandidates, sel)) {
+      for (int dd = 0; dd < 2; ++dd)
+        for (int i = 0; i < 3; ++i)
+          ctx->coh_lines[3 * dd + i] = ctx->coh_pool + kCohortMapWords + (size_t)sel[dd][i] * kLineWords;
+      ctx->coh_state = 1;
+    }
+  }
+  return ctx->coh_state == 1;
+}
 
 static int ensure(void** p, size_t* cap, size_t bytes) {
   if (*cap >= bytes) return HS_OK;
@@ -399,6 +426,7 @@ extern "C" int hs_ctx_destroy(hs_ctx* c) {
     if (ev) cudaEventDestroy(ev);
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   if (c->gstream) cudaStreamDestroy(c->gstream);
+  cudaFree(c->coh_pool);
   delete c;
   return HS_OK;
 }
@@ -595,6 +623,17 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c0, void* storage, int o
   d.cluster = cluster;
   d.variant = variant;
   r->cluster = cluster;
+  // global spin / FA mutex with more than one TB: the die-aware cohort lock
+  if ((c->prim == 4 || c->prim == 7) && c->num_tbs > 1 && !(c->flags & HS_RUN_NO_COHORT) &&
+      cohort_ready(ctx)) {
+    d.cohort = 1;
+    d.die_map = reinterpret_cast<const unsigned char*>(ctx->coh_pool);
+    for (int i = 0; i < 6; ++i) {
+      d.coh[i] = ctx->coh_lines[i];
+      if (!(c->flags & HS_RUN_KEEP_STATE)) HS_CK(cudaMemsetAsync(d.coh[i], 0, kLineWords * 4, st));
+    }
+    r->cohort = 1;
+  }
   cudaLaunchConfig_t lc = {};
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;

@@ -50,6 +50,11 @@ struct RunDesc {
   int l_lflag;          // per-group member flags (dense), lflag_lines per group
   int lflag_lines;
   int variant;          // HIP-extension variant of the primitive (PrimVariant)
+  // Cohort (die-aware) global mutexes: cohort != 0 enables them.  die_map[smid]
+  // is the SM's die (0/1); coh[3 * die + i] are three lock lines homed on that die.
+  int cohort;
+  const unsigned char* die_map;
+  unsigned* coh[6];
 };
 
 // Variants the HIP build of the reference adds to the CUDA primitives
@@ -63,6 +68,12 @@ enum PrimVariant : int {
   PV_NAIVE = 3,      // *NaiveSRB: every TB joins one global barrier (no local stage)
   PV_NAIVE_ALL = 4,  // *NaiveAllSRB: every thread joins one global barrier
 };
+
+// Cohort pool (one per context): a die map of 256 bytes (one per SM id), then
+// candidate lock lines whose home die calibration finds (hs_cohort.cu).
+constexpr int kCohortMapWords = 64;
+constexpr int kCohortCandidates = 128;
+bool hs_cohort_calibrate(int device, unsigned* pool, int ncand, int sel[2][3]);
 
 // Lock-state layout for a run: line offsets and total size.
 struct Layout {

@@ -32,6 +32,30 @@ template <int S, int KIND, int MODE, int V, bool TMA>
 __device__ __forceinline__ void mutex_loop(const RunDesc& d, int g, int r, int m, int G, unsigned* w0, unsigned* w1,
                                            unsigned* w2, unsigned* ring, unsigned ring_max, unsigned wrap,
                                            int* s_slot, TmaCtx& tma, const HsEnv& env) {
+  if constexpr (S == GPU && (KIND == MK_SPIN || KIND == MK_FA)) {
+    if (d.cohort) {  // global mutex as a cohort of per-die locks (hs_device.cuh)
+      unsigned sm;
+      asm volatile("mov.u32 %0, %%smid;" : "=r"(sm));
+      const int die = d.die_map[sm & 255u] & 1;
+      unsigned* const* c = d.coh + 3 * die;
+      unsigned my = 0, pc = 0, aux = 0;  // meaningful in the master thread
+      for (int j = 0; j < d.iters; ++j) {
+        bool ok;
+        if constexpr (KIND == MK_FA)
+          ok = cohort_ticket_lock(c[0], c[1], w0, w1, wrap, d.bo_unit, d.bo_max, env, my, pc, aux);
+        else
+          ok = cohort_tas_lock(c[0], w0, env, pc, aux);
+        if (!ok) break;
+        if constexpr (MODE == M_SLICE) cs_slice(d.data, g + ((r + j) % m) * G, d.L);
+        else if constexpr (TMA) ok = cs_chunk_tma<MODE>(d, g, tma, env);
+        else cs_chunk<MODE, V>(d, g);
+        if constexpr (KIND == MK_FA) cohort_ticket_unlock(c[1], w1, wrap, my, pc, aux);
+        else cohort_tas_unlock(c[0], w0, pc, aux);
+        if (!ok) break;
+      }
+      return;
+    }
+  }
   for (int j = 0; j < d.iters; ++j) {
     bool ok;
     int slot = 0;

@@ -48,8 +48,10 @@ enum {
   HS_RUN_KEEP_STATE = 2,  /* do not re-initialise lock state before the repeats */
   HS_RUN_NO_CLUSTER = 4,  /* tree barriers: keep the local stage in L2 instead of on thread-block clusters */
   HS_RUN_REGISTER_CS = 8, /* critical sections on the register path only (no bulk copies through shared memory) */
-  HS_RUN_GRAPH = 16       /* the repeats as one CUDA graph: captured once per context and launch shape, then
+  HS_RUN_GRAPH = 16,      /* the repeats as one CUDA graph: captured once per context and launch shape, then
                              replayed (not with HS_RUN_SYNC_EACH); the lock state is still reset before it */
+  HS_RUN_NO_COHORT = 32   /* global spin / EBO / FA mutexes: one lock word for the whole GPU instead of the
+                             die-aware cohort (a lock per die, homed on it, handed on within the die) */
 };
 
 /* One run of one SyncPrims primitive: `repeats` launches of `num_tbs` TBs of
@@ -81,6 +83,7 @@ typedef struct hs_run_result {
   unsigned long long ops;       /* num_tbs * num_iters * repeats */
   unsigned launches;            /* kernels launched by this call */
   int cluster;                  /* tree barriers: CTAs per thread-block cluster (1: no clusters) */
+  int cohort;                   /* global mutexes: 1 if the die-aware cohort lock ran */
 } hs_run_result;
 
 typedef struct hs_ctx hs_ctx;

@@ -113,6 +113,12 @@ template <int S> __device__ __forceinline__ unsigned atom_cas_acquire(unsigned* 
   else asm volatile("atom.acquire.gpu.cas.b32 %0, [%1], %2, %3;" : "=r"(o) : "l"(p), "r"(cmp), "r"(val) : "memory");
   return o;
 }
+template <int S> __device__ __forceinline__ unsigned atom_cas_release(unsigned* p, unsigned cmp, unsigned val) {
+  unsigned o;
+  if constexpr (S == CLUSTER) asm volatile("atom.release.cluster.cas.b32 %0, [%1], %2, %3;" : "=r"(o) : "l"(p), "r"(cmp), "r"(val) : "memory");
+  else asm volatile("atom.release.gpu.cas.b32 %0, [%1], %2, %3;" : "=r"(o) : "l"(p), "r"(cmp), "r"(val) : "memory");
+  return o;
+}
 template <int S> __device__ __forceinline__ unsigned atom_or_relaxed(unsigned* p, unsigned v) {
   unsigned o;
   if constexpr (S == CLUSTER) asm volatile("atom.relaxed.cluster.or.b32 %0, [%1], %2;" : "=r"(o) : "l"(p), "r"(v) : "memory");
@@ -245,6 +251,117 @@ template <int S>
 __device__ __forceinline__ void ticket_unlock(unsigned* turn, unsigned wrap) {
   __syncthreads();
   if (is_master()) red_release_inc<S>(turn, wrap);
+}
+
+// ---------------------------------------------------------------------------
+// Cohort (die-aware) mutexes.  A GB300 has two dies; an L2 line is homed on
+// one of them.  A lock hand-off between two SMs of the die that homes the lock
+// word costs ~450 ns, any hand-off that crosses the dies ~750 ns (and an
+// atomic ~150 against ~330 ns).  A cohort lock keeps hand-offs on one die: each
+// die has a local lock homed on it, and the global lock (the primitive's own
+// word) is taken only by a TB that did not inherit it.  A releasing holder
+// with local waiters passes the local lock together with the global one, at
+// most kCohortMaxPass times in a row; otherwise it releases both.  Mutual
+// exclusion is the global lock's (held by one cohort) and the local lock's
+// (one holder in the cohort).
+// ---------------------------------------------------------------------------
+constexpr unsigned kCohortMaxPass = 32;
+
+// Test-and-set cohort: the local word packs [31:16] waiters, [15:1] passes so
+// far (0: the cohort does not hold the global lock), [0] held.  The global
+// word is a test-and-set lock.  The acquiring CAS returns the waiter count,
+// so the holder knows at acquisition whether anyone on its die waits (a
+// registered waiter keeps waiting until it holds the lock); the release is
+// then one red.release.add: +1 turns "held, pc" into "free, pc + 1" (pass),
+// -(2 pc + 1) into "free, 0" (after the global release).
+__device__ __forceinline__ bool cohort_tas_lock(unsigned* local, unsigned* global, const HsEnv& env, unsigned& pc,
+                                                unsigned& others) {
+  int ok = 0;
+  if (is_master()) {
+    atomicAdd(local, 1u << 16);  // register as a waiter
+    unsigned got = 0;
+    ok = wait_until(
+        [&] {
+          const unsigned v = ld_relaxed<GPU>(local);
+          if (v & 1u) return false;
+          if (atom_cas_acquire<GPU>(local, v, (v | 1u) - (1u << 16)) != v) return false;
+          got = v;
+          return true;
+        },
+        [] {}, env, HS_SITE_SPIN_LOCK);
+    pc = (got >> 1) & 0x7FFFu;
+    others = (got >> 16) - 1u;
+    if (ok && pc == 0u)
+      ok = wait_until([&] { return ld_relaxed<GPU>(global) == 0u && atom_cas_acquire<GPU>(global, 0u, 1u) == 0u; },
+                      [] {}, env, HS_SITE_SPIN_LOCK);
+  }
+  return __syncthreads_or(ok) != 0;
+}
+__device__ __forceinline__ void cohort_tas_unlock(unsigned* local, unsigned* global, unsigned pc, unsigned others) {
+  __syncthreads();  // every thread's critical-section stores precede the release
+  if (is_master()) {
+    if (others != 0u && pc + 1u < kCohortMaxPass) {
+      red_release_add<GPU>(local, 1u);
+    } else {
+      st_release<GPU>(global, 0u);
+      red_release_add<GPU>(local, 0u - (2u * pc + 1u));
+    }
+  }
+}
+
+// Ticket cohort: a ticket lock per die over the global ticket lock.  The local
+// turn word carries the pass count: turn = (ticket << 6) | passes, written
+// only by the holder; local tickets wrap at kCohortTicketWrap.  The holder
+// snapshots the local ticket counter as soon as it holds the lock, so the
+// waiter check costs nothing at release.
+constexpr unsigned kCohortTicketWrap = (1u << 25) - 1u;
+__device__ __forceinline__ bool cohort_ticket_lock(unsigned* lt, unsigned* lu, unsigned* gt, unsigned* gu,
+                                                   unsigned wrap, unsigned unit, unsigned bmax, const HsEnv& env,
+                                                   unsigned& my, unsigned& pc, unsigned& snap) {
+  int ok = 0;
+  if (is_master()) {
+    my = atom_inc_relaxed<GPU>(lt, kCohortTicketWrap);
+    unsigned cur = 0;
+    ok = wait_until_p([&] { cur = ld_acquire<GPU>(lu); return (cur >> 6) == my; }, [&] { return cur; },
+                      [&] {
+                        if (unit) {
+                          const unsigned t = cur >> 6;
+                          const unsigned ahead = (my >= t) ? (my - t) : (my + kCohortTicketWrap + 1u - t);
+                          const unsigned ns = ahead > 1u ? (ahead - 1u) * unit : 0u;
+                          sleep_ns(ns < bmax ? ns : bmax);
+                        }
+                      },
+                      env, HS_SITE_FA_LOCK);
+    pc = cur & 63u;
+    snap = ld_relaxed<GPU>(lt);  // tickets taken so far; its value is needed only at release
+    if (ok && pc == 0u) {
+      const unsigned g = atom_inc_relaxed<GPU>(gt, wrap);
+      unsigned gc = 0;
+      ok = wait_until_p([&] { gc = ld_acquire<GPU>(gu); return gc == g; }, [&] { return gc; },
+                        [&] {
+                          if (unit) {
+                            const unsigned ahead = (g >= gc) ? (g - gc) : (g + wrap + 1u - gc);
+                            const unsigned ns = ahead > 1u ? (ahead - 1u) * unit : 0u;
+                            sleep_ns(ns < bmax ? ns : bmax);
+                          }
+                        },
+                        env, HS_SITE_FA_LOCK);
+    }
+  }
+  return __syncthreads_or(ok) != 0;
+}
+__device__ __forceinline__ void cohort_ticket_unlock(unsigned* lu, unsigned* gu, unsigned wrap, unsigned my,
+                                                     unsigned pc, unsigned snap) {
+  __syncthreads();
+  if (is_master()) {
+    const unsigned next = (my >= kCohortTicketWrap) ? 0u : my + 1u;
+    if (snap != next && pc + 1u < kCohortMaxPass) {
+      st_release<GPU>(lu, (next << 6) | (pc + 1u));  // pass the global lock on within the die
+    } else {
+      red_release_inc<GPU>(gu, wrap);
+      st_release<GPU>(lu, next << 6);
+    }
+  }
 }
 
 // Ring-buffer (array queue) "sleep" mutex.  A waiter takes slot
