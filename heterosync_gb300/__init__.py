@@ -32,6 +32,7 @@ _MODES = {"ref": MODE_REF, "inc": MODE_INC, "slice": MODE_SLICE}
 
 HS_OK, HS_EINVAL, HS_ETIMEDOUT, HS_ENORES, HS_ECUDA, HS_ENODEV, HS_EMISMATCH = range(7)
 RUN_SYNC_EACH, RUN_KEEP_STATE, RUN_NO_CLUSTER, RUN_REGISTER_CS, RUN_GRAPH, RUN_NO_COHORT = 1, 2, 4, 8, 16, 32
+RUN_CLUSTER_CS = 64
 
 # Reference names and ids, main.cu:1224-1256.
 PRIM_NAMES = {

@@ -16,6 +16,7 @@ namespace hs {
 using KernelFn = void (*)(RunDesc);
 KernelFn syncprim_plan(int prim, int mode, int threads, int num_ldst, size_t* smem_bytes, bool bulk = true);
 cudaError_t prepare_smem(KernelFn fn, size_t smem_bytes);
+KernelFn prim_cluster_kernel(int mode);
 cudaError_t launch_ring_init(unsigned* ring, unsigned slots_per_group, unsigned groups, cudaStream_t st);
 cudaError_t launch_fill_lines(unsigned* base, size_t n, size_t stride, unsigned value, cudaStream_t st);
 }  // namespace hs
@@ -609,6 +610,51 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c0, void* storage, int o
     }
   }
 
+  // Global mutexes and semaphores with a bulk-copy critical section: one
+  // cluster of m CTAs per logical TB, the critical section split over its SMs
+  // (m = 8, or fewer when the TB has fewer half-warp regions).  Measured at
+  // numLdSt 100 (reference mode, us per op, cluster against flat): faster
+  // only where a semaphore writer moves 4 or more chunks (spinSem1 at 608 TBs
+  // 4.72 against 5.40); slower for mutexes (faMutex 4.34 against 3.26) and
+  // smaller writers, so by default only there.
+  int grid = c->num_tbs;
+  const bool sem_prim = c->prim >= 8 && c->prim <= 15;
+  const int sem_numSM = c->num_tbs < nsm ? c->num_tbs : nsm;
+  const int sem_k = sem_prim ? (c->num_tbs + sem_numSM - 1) / sem_numSM : 1;  // chunks a semaphore writer owns
+  if (c->prim >= 4 && c->prim <= 15 && c->mode != HS_MODE_SLICE && c->num_ldst > 32 && c->threads <= 256 &&
+      !(c->flags & (HS_RUN_NO_CLUSTER | HS_RUN_REGISTER_CS)) && ((c->flags & HS_RUN_CLUSTER_CS) || sem_k >= 4)) {
+    const int R = c->threads / 16;
+    int m = 8;
+    while (m > R) m >>= 1;
+    KernelFn cfn = prim_cluster_kernel(c->mode);
+    if (m >= 2 && cfn) {
+      const int k = sem_k;
+      const size_t region = (size_t)64 * (c->num_ldst + 1);
+      size_t stage = (size_t)k * ((R + m - 1) / m) * region;      // a rank's share of every chunk: one tile
+      stage = std::min(stage, (size_t)(200 * 1024) / region * region);
+      cudaLaunchConfig_t lc = {};
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = (unsigned)m;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      lc.gridDim = dim3((unsigned)(c->num_tbs * m));
+      lc.blockDim = dim3((unsigned)c->threads);
+      lc.dynamicSmemBytes = stage;
+      lc.attrs = attr;
+      lc.numAttrs = 1;
+      int fit = 0;
+      if (stage >= region && prepare_smem(cfn, stage) == cudaSuccess &&
+          cudaOccupancyMaxActiveClusters(&fit, (const void*)cfn, &lc) == cudaSuccess && fit >= 1) {
+        fn = cfn;
+        smem = stage;
+        cluster = m;
+        grid = c->num_tbs * m;
+      }
+      cudaGetLastError();
+    }
+  }
+
   void* dev = storage;
   if (!on_device) {
     if ((s = ensure(&ctx->staging, &ctx->staging_cap, bytes + 16))) return r->status = s;
@@ -624,7 +670,7 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c0, void* storage, int o
   d.variant = variant;
   r->cluster = cluster;
   // global spin / FA mutex with more than one TB: the die-aware cohort lock
-  if ((c->prim == 4 || c->prim == 7) && c->num_tbs > 1 && !(c->flags & HS_RUN_NO_COHORT) &&
+  if ((c->prim == 4 || c->prim == 7) && c->num_tbs > 1 && grid == c->num_tbs && !(c->flags & HS_RUN_NO_COHORT) &&
       cohort_ready(ctx)) {
     d.cohort = 1;
     d.die_map = reinterpret_cast<const unsigned char*>(ctx->coh_pool);
@@ -640,7 +686,7 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c0, void* storage, int o
   attr[0].val.clusterDim.x = (unsigned)cluster;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
-  lc.gridDim = dim3((unsigned)c->num_tbs);
+  lc.gridDim = dim3((unsigned)grid);
   lc.blockDim = dim3((unsigned)c->threads);
   lc.dynamicSmemBytes = smem;
   lc.stream = st;

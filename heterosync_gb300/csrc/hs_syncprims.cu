@@ -18,7 +18,7 @@
 //  * every wait is bounded (see hs_device.cuh).
 #include <cuda_runtime.h>
 #include <cstdlib>
-#include "hs_cs.cuh"
+#include "hs_exec.cuh"
 
 namespace hs {
 
@@ -539,6 +539,42 @@ KernelFn syncprim_kernel(int prim, int mode, int threads, int num_ldst) {
 }
 
 // Allow the kernel its dynamic shared memory (once per function).
+// Global mutexes and semaphores with a bulk-copy critical section (numLdSt >
+// 32): one thread-block cluster per logical TB.  Rank 0 takes and releases the
+// lock or semaphore (the same words and rules as k_mutex / k_sem), and every
+// rank moves its slice of the chunk's half-warp regions through its own
+// bulk-copy engine (cl_mutex_op / cl_sem_op, shared with the batched kernel),
+// so one critical section's ~200 KB at numLdSt 100 moves over several SMs.
+// All ranks agree on every stop (cl_grant / cl_end), so none is left at a
+// cluster barrier.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_prim_cluster(RunDesc d) {
+  __shared__ int s_slot;
+  __shared__ int s_ok[1 + 8];
+  __shared__ unsigned long long s_mbar;
+  extern __shared__ __align__(128) unsigned char dyn_smem[];
+  TmaCtx tma;
+  tma_init(tma, &s_mbar, dyn_smem);
+  tma.cap = dyn_smem_bytes();
+  const HsEnv env{d.status, d.timeout_ns};
+  const int cl = d.cluster;
+  const int cr = (int)cluster_ctarank();
+  const int b = (int)blockIdx.x / cl;
+  const bool mutex = is_mutex_prim(d.prim);
+  for (int j = 0; j < d.iters; ++j) {
+    const bool ok = mutex ? cl_mutex_op<MODE>(d, b, cr, cl, &s_slot, s_ok, tma, env)
+                          : cl_sem_op<MODE>(d, b, cr, cl, s_ok, tma, env);
+    if (!ok) break;
+  }
+  cl_barrier(cl);  // rank 0's shared words stay valid until every rank is done
+}
+
+KernelFn prim_cluster_kernel(int mode) {
+  if (mode == M_REF) return k_prim_cluster<M_REF>;
+  if (mode == M_INC) return k_prim_cluster<M_INC>;
+  return nullptr;
+}
+
 cudaError_t prepare_smem(KernelFn fn, size_t smem_bytes) {
   if (smem_bytes <= 32 * 1024) return cudaSuccess;  // dynamic + static must stay under the 48 KB default
   return cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTmaMaxBytes);
