@@ -113,12 +113,6 @@ template <int S> __device__ __forceinline__ unsigned atom_cas_acquire(unsigned* 
   else asm volatile("atom.acquire.gpu.cas.b32 %0, [%1], %2, %3;" : "=r"(o) : "l"(p), "r"(cmp), "r"(val) : "memory");
   return o;
 }
-template <int S> __device__ __forceinline__ unsigned atom_cas_release(unsigned* p, unsigned cmp, unsigned val) {
-  unsigned o;
-  if constexpr (S == CLUSTER) asm volatile("atom.release.cluster.cas.b32 %0, [%1], %2, %3;" : "=r"(o) : "l"(p), "r"(cmp), "r"(val) : "memory");
-  else asm volatile("atom.release.gpu.cas.b32 %0, [%1], %2, %3;" : "=r"(o) : "l"(p), "r"(cmp), "r"(val) : "memory");
-  return o;
-}
 template <int S> __device__ __forceinline__ unsigned atom_or_relaxed(unsigned* p, unsigned v) {
   unsigned o;
   if constexpr (S == CLUSTER) asm volatile("atom.relaxed.cluster.or.b32 %0, [%1], %2;" : "=r"(o) : "l"(p), "r"(v) : "memory");
