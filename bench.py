@@ -15,6 +15,13 @@ the 6 points, so the default 6 timed steps cover the sweep once.
          buffers: host->device copy, lock-state init, launch, device->host copy
          and status read-back are inside the timed region
 
+  roofline      the dominant kernel's critical-section bytes against the measured HBM
+                copy rate (tiny by construction: the lock kernels are latency-bound)
+  l2_atomic     the sweep's algorithmic atomics against the contention-free L2 atomic rate
+  lock_latency  the measured hand-off, atomic and L2 load latencies, the per-op floor
+                they set for a CAS lock and a queue lock, and each numLdSt-10 lock
+                cell at NUM_SM TBs as a fraction of its floor
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
 Beside the sweep, outside its timed region, the line carries "fa_mutex_slice"
