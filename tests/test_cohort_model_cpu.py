@@ -1,0 +1,40 @@
+"""The cohort (die-aware) mutex protocols, modelled on the host: std::threads
+stand for TBs on two dies and run the device code's encodings (test-and-set
+with waiters and passes in one word; ticket with the pass count in the turn
+word).  Small ticket wraps and pass limits drive the wrap-around and global
+release branches.  Mutual exclusion must hold, every critical section must
+count, and every lock word must end free."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def model(tmp_path_factory):
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("g++ not found")
+    exe = str(tmp_path_factory.mktemp("cohort") / "cohort_model")
+    subprocess.run([cxx, "-std=c++17", "-O2", "-pthread", os.path.join(HERE, "cohort_model.cpp"), "-o", exe],
+                   check=True)
+    return exe
+
+
+@pytest.mark.parametrize("kind", ["tas", "ticket"])
+@pytest.mark.parametrize("threads,iters,max_pass,lwrap,gwrap", [
+    (4, 20000, 32, (1 << 25) - 1, 1000000000),  # the device's constants
+    (6, 20000, 2, 7, 5),                         # every other op crosses; tickets wrap constantly
+    (8, 10000, 32, 3, 1),
+    (3, 30000, 1, 6, 2),                         # max_pass 1: never passes, always the global lock
+])
+def test_cohort_protocol(model, kind, threads, iters, max_pass, lwrap, gwrap):
+    # a local wrap must exceed the threads that can hold tickets at once, as on the device (2^25 - 1)
+    if kind == "ticket" and lwrap + 1 < (threads + 1) // 2 + 1:
+        pytest.skip("wrap smaller than the waiters of one die")
+    p = subprocess.run([model, kind, str(threads), str(iters), str(max_pass), str(lwrap), str(gwrap)],
+                       capture_output=True, text=True, timeout=120)
+    assert p.returncode == 0 and p.stdout.startswith("ok %d" % (threads * iters)), p.stdout + p.stderr
