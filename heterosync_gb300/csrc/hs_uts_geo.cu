@@ -515,16 +515,14 @@ extern "C" int hs_uts_geo_coop_run(unsigned seed, int depth_limit, double branch
     try {
       pool.emplace_back(host_walker, std::ref(h), blocks == 0 && i == 0);
     } catch (...) {
-      if (i == 0 && blocks == 0) break;  // nobody holds the root: nothing ran
-      break;                             // fewer walkers: the others balance the load
+      break;  // fewer walkers: the others (and the GPU) balance the load
     }
   }
   const int ran = (int)pool.size();
-  if (ran == 0 && blocks == 0) {
+  if (ran == 0 && blocks == 0) {  // walker 0 would have held the root: nothing ran
     g_gerr = "could not start a host thread";
     return HS_ENORES;
   }
-  if (ran == 0 && host_threads > 0) __atomic_store_n(h.br.ctl + 32, 0u, __ATOMIC_RELEASE);
   for (auto& t : pool) t.join();
   cudaError_t e = cudaSuccess;
   unsigned ctl[256] = {0};
