@@ -77,7 +77,9 @@ __host__ __device__ __forceinline__ unsigned rotl32(unsigned x, int n) {
 // SHA-1 (FIPS 180-4) of one padded 64-byte block given as 16 big-endian words.
 __host__ __device__ __forceinline__ void sha1_block(unsigned w[16], unsigned h[5]) {
   unsigned a = 0x67452301u, b = 0xEFCDAB89u, c = 0x98BADCFEu, d = 0x10325476u, e = 0xC3D2E1F0u;
+#ifdef __CUDA_ARCH__
 #pragma unroll
+#endif
   for (int t = 0; t < 80; ++t) {
     unsigned wt;
     if (t < 16) {

@@ -207,7 +207,7 @@ int hs_batch_run(hs_batch* b, void* stream, hs_batch_result* result);
 /* Comparison point: one standalone launch per instance on the same stream. */
 int hs_batch_run_serial(hs_batch* b, void* stream, hs_batch_result* result);
 
-/* ---- relaxed-atomics microbenchmarks (cuda/relaxedAtomics/uvm/*) --------------- */
+/* ---- relaxed-atomics microbenchmarks (cuda/relaxedAtomics/uvm) ----------------- */
 /* Host arrays in and out (the reference's managed arrays); the kernel alone is
  * timed.  Sizes and array lengths are the reference's. */
 typedef struct hs_relaxed_result {
