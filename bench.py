@@ -1,45 +1,48 @@
 """Benchmark: sync ops/s of the SyncPrims hot path on GB300.
 
-Workload (the per-primitive sweep): 16 primitives -- spinMutex, spinMutexEBO,
-sleepMutex, faMutex, spinSem{1,2,10,120}, spinSemEBO{1,2,10,120},
-atomicTreeBarrUniq(LocalExch), lfTreeBarrUniq(LocalExch) -- at 256 threads/TB,
-numCSIters = 1000, numLdSt in {10, 100}, numTBs in {1, 2, 4} x NUM_SM (148, 296,
-592 on a 148-SM part; 152, 304, 608 here), seeded uint32 shared data moved by
-the reference's critical section (bit-exact final state).  One step = one launch
-of each of the 16 primitives at one (numTBs, numLdSt) point; steps cycle through
-the 6 points, so the default 6 timed steps cover the sweep once.
+Headline workload (both arms run exactly this): the 8 SyncPrims the
+reference's own CUDA build can run on GB300 -- spinMutex, spinMutexEBO,
+sleepMutex, faMutex, atomicTreeBarrUniq(LocalExch), lfTreeBarrUniq(LocalExch)
+-- at 256 threads/TB, numCSIters = 1000, numLdSt in {10, 100}, numTBs in
+{1, 2, 4} x NUM_SM (148, 296, 592 on a 148-SM part; 152, 304, 608 here), seeded
+uint32 shared data moved by the reference's critical section (bit-exact final
+state checked after every run).  One step = one launch of each of the 8
+primitives at one (numTBs, numLdSt) point; steps cycle through the 6 points.
 
-  value  sync ops/s = sum(numTBs * numCSIters) / sum(device time of the launches),
-         storage already resident in HBM (CUDA events on the launch stream)
-  e2e    the same ops / wall time of the C-ABI call hs_run() with pinned HOST
-         buffers: host->device copy, lock-state init, launch, device->host copy
-         and status read-back are inside the timed region
+  value  sync ops/s over the sweep: every (primitive, point) cell carries its
+         numTBs * 1000 ops at its mean device time over the steps that ran it
+         (so the figure does not depend on how often the step count visits each
+         point); storage already resident in HBM, CUDA events on the launch stream
+  e2e    the same, with each cell's wall time of the C-ABI call hs_run() on pinned
+         HOST buffers (host->device copy, lock-state init, launch, device->host
+         copy and status read-back inside the timed region)
 
-  roofline      the dominant kernel's critical-section bytes against the measured HBM
-                copy rate (tiny by construction: the lock kernels are latency-bound)
-  l2_atomic     the sweep's algorithmic atomics against the contention-free L2 atomic rate
-  lock_latency  the measured hand-off, atomic and L2 load latencies, the per-op floor
-                they set for a CAS lock and a queue lock, and each numLdSt-10 lock
-                cell at NUM_SM TBs as a fraction of its floor
+  roofline      bound "latency": the dominant kernel (k_mutex) against its
+                measured per-op floor, one lock hand-off plus one uncontended
+                operation of the same primitive and numLdSt (see lock_floors)
+  full_sweep    the 16-primitive sweep (the 8 above plus spinSem{1,2,10,120} and
+                spinSemEBO{1,2,10,120}) once over the 6 points, outside the timed
+                region; the reference's semaphore kernels cannot run on GB300
+  per_cell_vs_reference  this arm's us/op against the reference arm's, per cell,
+                when the reference arm ran on this machine just before
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
 Beside the sweep, outside its timed region, the line carries "fa_mutex_slice"
 (faMutex, 8 TBs, numLdSt 10, 100 iterations: the one-launch slice workload),
-"exchange" (tree
-barrier with local exchange on thread-block clusters: 592 CTAs, fp32[4096] per
-CTA rotated every episode, 1000 episodes, cluster sizes 1/2/4/8) and "batch"
-(the 64-instance mixed batch, one launch per instance against the autotuned
-persistent graph-replayed launch) and "serve" (the served request loop: peak
-request rate, p50/p99 latency under Poisson arrivals at 10-90% of it) and
-"uts_geo" (geometric SHA-1 UTS, depth 12, nodes/s, on the GPU alone and
-with the host cores walking the same tree cooperatively); the
-extras run outside the sweep's timed region; --no-extras skips them.
+"exchange" (tree barrier with local exchange on thread-block clusters: 592
+CTAs, fp32[4096] per CTA rotated every episode, 1000 episodes, cluster sizes
+1/2/4/8), "batch" (the 64-instance mixed batch, one launch per instance against
+the autotuned persistent graph-replayed launch), "serve" (the served request
+loop: sustained request rate, p50/p99 latency and slowdown under Poisson
+arrivals at 10-90% of it) and "uts_geo" (geometric SHA-1 UTS, depth 12,
+nodes/s, on the GPU alone and with the host cores walking the same tree);
+--no-extras skips them.
 
 --impl reference runs the reference's own SyncPrims kernels (built from its
-unmodified sources into oracle/_ref) on the same GPU with the same sizes, each
-step a bounded sample (fewer iterations); without oracle/_ref it falls back to
-the host std::thread port.  Multi-GPU: replicas only (each rank runs the whole
+unmodified sources into oracle/_ref) on the same GPU, on the same cells, at the
+same numCSIters = 1000 (no projection); without oracle/_ref it falls back to the
+host std::thread port.  Multi-GPU: replicas only (each rank runs the whole
 sweep on its own GPU; no data crosses GPUs).
 """
 from __future__ import annotations
@@ -64,26 +67,42 @@ SWEEP_PRIMS = ["spinMutex", "spinMutexEBO", "sleepMutex", "faMutex",
                "atomicTreeBarrUniq", "atomicTreeBarrUniqLocalExch", "lfTreeBarrUniq", "lfTreeBarrUniqLocalExch"]
 # The reference's global semaphore kernels are not run (they can wait forever
 # on GB300: each CTA reads maxSemCount from the live count at kernel start), so
-# the reference arm covers the mutexes and barriers; the build's line also
-# reports that same subset ("same_subset").
-REF_PRIMS = [p for p in SWEEP_PRIMS if "Sem" not in p]
+# the headline workload -- the one both arms run -- is the mutexes and barriers.
+HEAD_PRIMS = [p for p in SWEEP_PRIMS if "Sem" not in p]
+SEM_PRIMS = [p for p in SWEEP_PRIMS if "Sem" in p]
 REF_EXCLUDED = ("not run: each CTA of the reference's semaphore kernels reads maxSemCount from the live "
                 "count word at kernel start (main.cu:542-543, 695-696); a late writer that reads 0 can wait "
                 "forever, and a run that launched them did not finish")
 THREADS = 256
 ITERS = 1000
+WARM_ITERS = 20
 LDST = (10, 100)
 TB_MULT = (1, 2, 4)
 SEED = 20260101
+# where the reference arm leaves its per-cell times for the build arm run next on the same machine
+REF_CELLS_FILE = os.path.join(tempfile.gettempdir(), "hs_reference_cells.json")
 
 
-# DRAM bytes (read + write) of one launch of the dominant sweep kernel, from
-# one ncu capture (spinSem1, 152 TBs x 256 threads, numLdSt 100): the chunk and
-# the lock word stay L2-resident, so DRAM traffic is the cold first read and
-# does not grow with the launch's operations.
-DRAM_BYTES_PER_LAUNCH = 120000
-TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_sem (spinSem1, 152 TBs, numLdSt 100); "
-                  "profiles/k_sem_spinSem1_152tbs_L100.md")
+# DRAM bytes (read + write) of one launch of the dominant headline kernel, from
+# one ncu capture (k_mutex, spinMutex, 152 TBs x 256 threads, numLdSt 100): the
+# chunk and the lock word stay L2-resident, so DRAM traffic is the cold first
+# read and does not grow with the launch's operations.
+DRAM_BYTES_PER_LAUNCH = 140032 + 19456
+TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_mutex (spinMutex, 152 TBs x 256, numLdSt 100, "
+                  "200 iterations); profiles/k_mutex_spinMutex_152tbs_L100.md")
+
+
+def head_config(nsm):
+    """The headline workload's description: the same object in both arms' lines."""
+    return {"workload": "SyncPrims sweep: spinMutex, spinMutexEBO, sleepMutex, faMutex, atomicTreeBarrUniq(LocalExch), "
+                        "lfTreeBarrUniq(LocalExch) x numTBs {%s} x numLdSt {10,100}, 256 threads/TB, numCSIters 1000, "
+                        "reference critical section on seeded uint32 data"
+                        % ",".join(str(m * nsm) for m in TB_MULT),
+            "threads": THREADS, "num_iters": ITERS, "num_ldst": list(LDST),
+            "num_tbs": [m * nsm for m in TB_MULT], "primitives": HEAD_PRIMS,
+            "step": "one launch of each primitive at one (numTBs, numLdSt) point; steps cycle the 6 points; "
+                    "each cell counts at its mean time over the steps that ran it",
+            "l2": "flushed before every run (256 MiB write)"}
 
 
 def sweep_points(nsm):
@@ -160,12 +179,12 @@ def pinned_like(arr):
     return t, a
 
 
-def run_step(hs, nsm, point, iters, check, flush):
-    """One step: every sweep primitive at one (numTBs, numLdSt) point through
-    hs_run with pinned host storage.  Returns per-run records."""
+def run_cells(hs, prims, point, iters, check, flush):
+    """Every primitive of `prims` at one (numTBs, numLdSt) point through hs_run
+    with pinned host storage.  Returns per-run records."""
     G, L = point
     recs = []
-    for name in SWEEP_PRIMS:
+    for name in prims:
         cfg = hs.RunConfig(prim=name, num_ldst=L, num_tbs=G, num_iters=iters, threads=THREADS, repeats=1,
                            mode="ref")
         words = hs.storage_words(cfg)
@@ -181,19 +200,45 @@ def run_step(hs, nsm, point, iters, check, flush):
                 raise SystemExit("bench: %s numTBs=%d numLdSt=%d differs from the expected final state"
                                  % (name, G, L))
         recs.append({"prim": name, "num_tbs": G, "num_ldst": L, "iters": iters, "ops": r.ops,
-                     "ms": r.elapsed_ms, "wall_s": wall, "bytes": words * 4, "launches": r.launches})
+                     "ms": r.elapsed_ms, "wall_s": wall, "bytes": words * 4, "launches": r.launches,
+                     "cohort": r.cohort, "cluster": r.cluster})
     return recs
 
 
-def cpu_baseline(nsm, budget_s=15.0):
+def cell_key(prim, G, L):
+    return "%s@%d/%d" % (prim, G, L)
+
+
+def aggregate(recs):
+    """Per-cell means over the runs of each (primitive, numTBs, numLdSt) cell,
+    and the sweep rate: sum of the cells' ops over the sum of their mean times."""
+    cells = {}
+    for r in recs:
+        c = cells.setdefault(cell_key(r["prim"], r["num_tbs"], r["num_ldst"]),
+                             {"prim": r["prim"], "num_tbs": r["num_tbs"], "num_ldst": r["num_ldst"], "ops": r["ops"],
+                              "ms": [], "wall_s": []})
+        c["ms"].append(r["ms"])
+        c["wall_s"].append(r.get("wall_s", 0.0))
+    for c in cells.values():
+        c["mean_ms"] = sum(c["ms"]) / len(c["ms"])
+        c["mean_wall_s"] = sum(c["wall_s"]) / len(c["wall_s"])
+        c["us_per_op"] = c["mean_ms"] * 1e3 / c["ops"]
+    ops = sum(c["ops"] for c in cells.values())
+    ms = sum(c["mean_ms"] for c in cells.values())
+    wall = sum(c["mean_wall_s"] for c in cells.values())
+    return cells, (ops / (ms * 1e-3) if ms else None), (ops / wall if wall else None)
+
+
+def cpu_baseline(nsm, prims=None, budget_s=15.0):
     """Host std::thread port (the oracle twins) on a bounded sample of the same
     sweep: every (primitive, numTBs, numLdSt) cell, each with an untimed
     5-iteration pilot and then a timed run whose iteration count spreads
     `budget_s` of CPU work evenly over the cells (at most 1000 iterations)."""
     import oracle
     import heterosync_gb300 as hs
+    prims = prims or HEAD_PRIMS
     cores = os.cpu_count() or 1
-    cells = [(name, G, L) for (G, L) in sweep_points(nsm) for name in SWEEP_PRIMS]
+    cells = [(name, G, L) for (G, L) in sweep_points(nsm) for name in prims]
     per_cell = budget_s / len(cells)
     total_ops, total_s, iters_used = 0, 0.0, []
     for name, G, L in cells:
@@ -208,8 +253,8 @@ def cpu_baseline(nsm, budget_s=15.0):
         iters_used.append(it)
     return {"value": total_ops / total_s if total_s else None, "unit": "sync ops/s", "cores": cores,
             "kind": "port",
-            "sample": "host std::thread twins over all %d sweep cells, numCSIters %d-%d per cell (pilot-scaled, "
-                      "~%.0f s of CPU work), each cell's rate projected to its numTBs*1000 ops"
+            "sample": "host std::thread twins over the %d cells of the headline sweep, numCSIters %d-%d per cell "
+                      "(pilot-scaled, ~%.0f s of CPU work), each cell's rate projected to its numTBs*1000 ops"
                       % (len(cells), min(iters_used), max(iters_used), budget_s)}
 
 
@@ -224,38 +269,76 @@ def l2_atomic_peak(hs):
     return v.value, same.value
 
 
-# The lock kernels' latency floor per op, from the measured hand-off latencies:
-# a CAS lock's next holder sees the release (one hand-off), wins its atomic,
-# loads its critical section and waits for its stores' ack before releasing;
-# a queue lock (ticket, ring slot) takes its place in advance, so no atomic
-# sits on the chain.
+# How a lock op's chain runs under contention.  A CAS lock's next holder sees
+# the release (one hand-off), wins its atomic, runs the critical section and
+# releases; a queue lock (ticket, ring slot) takes its place ahead of time, so
+# no atomic sits on the chain.
 LOCK_CHAIN = {"spinMutex": "cas", "spinMutexEBO": "cas", "faMutex": "queue", "sleepMutex": "queue",
               "spinSem1": "cas", "spinSem2": "cas", "spinSem10": "cas", "spinSem120": "cas",
               "spinSemEBO1": "cas", "spinSemEBO2": "cas", "spinSemEBO10": "cas", "spinSemEBO120": "cas"}
 
 
-def lock_latency(hs, recs, nsm):
-    """Per-op latency floor of each lock cell at numTBs = NUM_SM, numLdSt 10
-    (where every semaphore TB is a writer and the op is a pure hand-off),
-    against the measured time per op."""
+def lock_floors(hs, prims):
+    """The per-op latency floor of each serialised lock primitive at each
+    numLdSt, from measurements on this GPU:
+
+        floor(L) = hand-off + 2 x L2 load + (CAS lock ? atomic : 0) + (t1(L) - t1(10))
+
+    The first three terms are the chain of one contended op at numLdSt 10: the
+    next holder sees the release (the median one-way flag latency between two
+    SMs), wins its atomic (a queue lock took its ticket or slot ahead of time),
+    loads its critical section and waits for its stores before releasing (two
+    L2 round trips).  The last term is the extra critical-section time of a
+    larger numLdSt: t1(L) is the time per op of the same primitive run by ONE TB
+    (1000 uncontended rounds), so t1(L) - t1(10) is the data movement one SM
+    adds, which no hand-off hides."""
     lat = hs.probe_latency(256)
     h, a, ld = lat["handoff_ns_median"], lat["atomic_rtt_ns"], lat["load_rtt_ns"]
-    floor = {"cas": h + a + 2 * ld, "queue": h + 2 * ld}
-    cells = {}
-    for r in recs:
-        if r["prim"] in LOCK_CHAIN and r["num_tbs"] == nsm and r["num_ldst"] == 10:
-            us = r["ms"] * 1e3 / r["ops"]
-            f = floor[LOCK_CHAIN[r["prim"]]] * 1e-3
-            cells.setdefault(r["prim"], []).append((us, f))
-    return {"handoff_ns": {"median": h, "min": lat["handoff_ns_min"], "max": lat["handoff_ns_max"],
-                           "partners": lat["partners"]},
-            "atomic_rtt_ns": a, "load_rtt_ns": ld,
-            "floor_ns": {"cas_lock": floor["cas"], "queue_lock": floor["queue"]},
-            "model": "cas lock: hand-off + atomic + CS load + store ack (2 x L2 load); queue lock: no atomic",
-            "cells_152x10": {k: {"us_per_op": round(sum(u for u, _ in v) / len(v), 3),
-                                 "floor_us": round(v[0][1], 3),
-                                 "frac": round(v[0][1] / (sum(u for u, _ in v) / len(v)), 3)}
-                             for k, v in cells.items()}}
+    t1 = {}
+    for name in prims:
+        if name not in LOCK_CHAIN:
+            continue
+        for L in LDST:
+            cfg = hs.RunConfig(prim=name, num_ldst=L, num_tbs=1, num_iters=ITERS, threads=THREADS, repeats=1,
+                               mode="ref")
+            init = make_init(hs.storage_words(cfg), SEED)
+            best = None
+            for _ in range(3):
+                r = hs.run(cfg, init.copy())
+                us = r.elapsed_ms * 1e3 / r.ops
+                best = us if best is None else min(best, us)
+            t1[(name, L)] = best
+    base = {"cas": h + a + 2 * ld, "queue": h + 2 * ld}
+    floors = {}
+    for (name, L), v in t1.items():
+        extra = max(0.0, v - t1[(name, LDST[0])]) * 1e3 if (name, LDST[0]) in t1 else 0.0
+        floors[(name, L)] = (base[LOCK_CHAIN[name]] + extra) * 1e-3
+    return floors, {"handoff_ns": {"median": h, "min": lat["handoff_ns_min"], "max": lat["handoff_ns_max"],
+                                   "partners": lat["partners"]},
+                    "atomic_rtt_ns": a, "load_rtt_ns": ld,
+                    "floor_ns": {"cas_lock": base["cas"], "queue_lock": base["queue"]},
+                    "uncontended_us_per_op": {"%s/%d" % k: round(v, 4) for k, v in t1.items()},
+                    "floor_us_per_op": {"%s/%d" % k: round(v, 4) for k, v in floors.items()},
+                    "model": "floor = hand-off + 2 x L2 load + (CAS lock: atomic) + t1(numLdSt) - t1(10); t1 = one "
+                             "TB's uncontended time per op"}
+
+
+def latency_roofline(cells, floors, kernel_prims, traffic):
+    """bound "latency": the dominant kernel's cells against their floors.
+    achieved = its ops / its time; peak = the same ops at the floor per op."""
+    sel = [c for c in cells.values() if c["prim"] in kernel_prims and (c["prim"], c["num_ldst"]) in floors]
+    ops = sum(c["ops"] for c in sel)
+    ms = sum(c["mean_ms"] for c in sel)
+    floor_ms = sum(c["ops"] * floors[(c["prim"], c["num_ldst"])] * 1e-3 for c in sel)
+    achieved = ops / (ms * 1e-3)
+    peak = ops / (floor_ms * 1e-3)
+    return {"bound": "latency", "kernel": "k_mutex", "achieved": achieved, "peak": peak, "unit": "sync ops/s",
+            "frac": achieved / peak, "peak_source": "measured (hs_probe_latency hand-off + uncontended op)",
+            "traffic": traffic, "traffic_source": TRAFFIC_SOURCE,
+            "cells": {cell_key(c["prim"], c["num_tbs"], c["num_ldst"]):
+                      {"us_per_op": round(c["us_per_op"], 4), "floor_us": round(floors[(c["prim"], c["num_ldst"])], 4),
+                       "frac": round(floors[(c["prim"], c["num_ldst"])] / c["us_per_op"], 3)} for c in sel},
+            "formula": "frac = sum(ops * floor_us) / sum(ops * us_per_op) over the dominant kernel's cells"}
 
 
 # algorithmic L2 atomics per sync op (contention-free minimum of this build's
@@ -267,7 +350,7 @@ ATOMICS_PER_OP = {"spinMutex": 2, "spinMutexEBO": 2, "sleepMutex": 3, "faMutex":
                   "lfTreeBarrUniqLocalExch": 2}
 
 
-def cs_bytes(name, G, L, nsm):
+def cs_bytes(name, G, L, nsm, iters=ITERS):
     """Algorithmic bytes one launch moves: 4-byte load + 4-byte store per element
     touched by a critical section (T*numLdSt elements per mutex op; the writer's
     numTBs_perSM chunks per semaphore writer op, T*numLdSt loads per reader op;
@@ -276,13 +359,28 @@ def cs_bytes(name, G, L, nsm):
     k = -(-G // nsm)
     if "Barr" in name:
         per = 2 if ("LocalExch" in name and k > 1) else 1
-        return G * ITERS * T * L * 8 * per
+        return G * iters * T * L * 8 * per
     if "Sem" in name:
         numSM = min(G, nsm)
         writers = sum(1 for tb in range(G) if tb // numSM == (tb % numSM) % k)
         readers = G - writers
-        return ITERS * (writers * k * T * L * 8 + readers * T * L * 4)
-    return G * ITERS * T * L * 8
+        return iters * (writers * k * T * L * 8 + readers * T * L * 4)
+    return G * iters * T * L * 8
+
+
+def secondary_bounds(hs, cells, nsm, dev_s):
+    """The HBM and L2-atomic fractions of the same cells (both tiny by
+    construction: a serialised lock uses neither bandwidth nor atomic rate)."""
+    peak_gbs, peak_kind = load_peaks()
+    byts = sum(cs_bytes(c["prim"], c["num_tbs"], c["num_ldst"], nsm) for c in cells.values())
+    atom_peak, same_rate = l2_atomic_peak(hs)
+    atom = sum(c["ops"] * ATOMICS_PER_OP[c["prim"]] for c in cells.values()) / dev_s
+    return {"hbm": {"achieved": byts / dev_s / 1e9, "peak": peak_gbs, "unit": "GB/s",
+                    "frac": byts / dev_s / 1e9 / peak_gbs, "peak_source": peak_kind,
+                    "note": "critical-section bytes (L2-resident)"},
+            "l2_atomic": {"achieved": atom, "peak": atom_peak, "frac": (atom / atom_peak) if atom_peak else None,
+                          "unit": "atomics/s", "same_address_rate": same_rate,
+                          "note": "peak: contention-free red.add probe; same_address_rate: one word"}}
 
 
 def fa_mutex_slice_extra(hs, nsm):
@@ -438,72 +536,98 @@ def combine_ranks(dist, dev_s, e2e_s, ops, device):
     return mx[0].item(), mx[1].item(), int(sm[2].item())
 
 
-def reference_arm(args, rank):
+def gpu_identity():
+    try:
+        import torch
+        pr = torch.cuda.get_device_properties(torch.cuda.current_device())
+        return "%s/%s" % (pr.name, getattr(pr, "uuid", ""))
+    except Exception:  # noqa: BLE001
+        return ""
+
+
+def reference_arm(args, rank, flush):
+    """The reference's own SyncPrims kernels (sm_100 build of its unmodified
+    sources) on the headline cells, each run at numCSIters = 1000 and timed with
+    CUDA events around its launch (the reference's ROI, main.cu:1494-1619)."""
+    if rank != 0:
+        return None
     import oracle
-    hs_nsm = None
+    import heterosync_gb300 as hs
     out = {"impl": "reference", "metric": "sync ops/s", "unit": "sync ops/s", "higher_is_better": True,
            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "data": "synthetic",
            "dtype": "u32", "scaling": "weak", "vs_baseline": None}
-    if rank != 0:
-        return None
-    # Bounded sample with fixed iteration counts: the reference's semaphores take
-    # 0.1-0.4 ms per op under contention and its EBO readers' backoff grows
-    # without bound (cudaLocksSemaphoreEBO.cu:176), so their run time is not
-    # linear in numCSIters; each semaphore TB does one wait/post.
-    def iters_ref_for(name):
-        if "Barr" in name:
-            return 200
-        if "Sem" in name:
-            return 1
-        return 30
-    iters_ref = "per family: barriers 200, mutexes 30, semaphores 1"
     if oracle.ref_available(THREADS):
         nsm, _ = oracle.ref_device()
-        hs_nsm = nsm
         pts = sweep_points(nsm)
         recs = []
+        t_start = time.perf_counter()
         for step in range(args.warmup + args.steps):
             G, L = pts[step % len(pts)]
-            for name in REF_PRIMS:
-                import heterosync_gb300 as hs
+            timed = step >= args.warmup
+            it = ITERS if timed else WARM_ITERS
+            for name in HEAD_PRIMS:
                 p = hs.prim_id(name)
                 n = oracle.storage_words(p, THREADS, L, G, nsm)
                 init = make_init(n, SEED + G + L)
-                it = 1 if step < args.warmup else iters_ref_for(name)
-                _, ms = oracle.ref_run(p, THREADS, L, G, it, 1, init)
+                flush()
+                got, ms = oracle.ref_run(p, THREADS, L, G, it, 1, init)
                 print("reference %s numTBs=%d numLdSt=%d iters=%d: %.3f ms" % (name, G, L, it, ms), file=sys.stderr,
                       flush=True)
-                if step >= args.warmup:
-                    recs.append((G * it, ms, G * ITERS))
-        # same metric as the build's arm: each cell's measured rate carries the
-        # cell's full-workload ops (numTBs * 1000), and the sweep value is the
-        # full workload's ops over the sum of the projected cell times
-        ops = sum(full for _, _, full in recs)
-        ms = sum(m * full / o for o, m, full in recs)
-        value = ops / (ms * 1e-3)
-        out.update({"value": value, "ms_per_step": ms / args.steps,
-                    "config": {"workload": "per-primitive sweep, reference CUDA kernels (sm_100 build of the "
-                                           "unmodified sources) on this GPU",
-                               "threads": THREADS, "num_iters": iters_ref, "num_ldst": list(LDST),
-                               "num_tbs": [m * nsm for m in TB_MULT], "primitives": REF_PRIMS,
-                               "excluded": {"semaphores (spinSem*, spinSemEBO*)": REF_EXCLUDED},
-                               "sample": "each (primitive, size) launched once with numCSIters %s "
-                                         "(the build's arm uses %d)" % (iters_ref, ITERS)},
+                if timed:
+                    cfg = hs.RunConfig(prim=name, num_ldst=L, num_tbs=G, num_iters=it, threads=THREADS, repeats=1,
+                                       mode="ref")
+                    if not args.no_check and not np.array_equal(got, hs.expected_storage(cfg, init)):
+                        raise SystemExit("bench: the reference's %s numTBs=%d numLdSt=%d final state differs from "
+                                         "the closed form" % (name, G, L))
+                    recs.append({"prim": name, "num_tbs": G, "num_ldst": L, "ops": G * it, "ms": ms})
+        cells, value, _ = aggregate(recs)
+        per_cell = {k: round(c["us_per_op"], 4) for k, c in cells.items()}
+        try:
+            with open(REF_CELLS_FILE, "w") as f:
+                json.dump({"gpu": gpu_identity(), "time": time.time(), "us_per_op": per_cell}, f)
+        except OSError:
+            pass
+        out.update({"value": value, "ms_per_step": sum(r["ms"] for r in recs) / args.steps,
+                    "config": head_config(nsm),
+                    "reference_build": "reference SyncPrims kernels, sm_100 build of the unmodified sources "
+                                       "(oracle/_ref), run through the driver API with the reference's launch shape",
+                    "excluded": {"semaphores (spinSem*, spinSemEBO*)": REF_EXCLUDED},
+                    "per_cell_us_per_op": per_cell,
+                    "wall_s": time.perf_counter() - t_start,
                     "cpu_baseline": {"value": value, "unit": "sync ops/s", "cores": None, "kind": "reference",
-                                     "sample": "reference SyncPrims kernels on the GB300, %d sampled ops projected "
-                                               "to the sweep's %d" % (sum(o for o, _, _ in recs), ops)},
+                                     "sample": "the reference's CUDA kernels on this GPU (the reference has no CPU "
+                                               "implementation of its primitives): every headline cell at "
+                                               "numCSIters %d, no projection" % ITERS},
                     "e2e": {"value": value, "unit": "sync ops/s", "h2d_bytes_per_step": 0,
                             "d2h_bytes_per_step": 0}})
     else:
-        import heterosync_gb300 as hs
-        nsm = hs.device_info()["nsm"] if hs_nsm is None else hs_nsm
+        nsm = hs.device_info()["nsm"]
         cb = cpu_baseline(nsm)
-        out.update({"value": cb["value"], "ms_per_step": None,
-                    "config": {"workload": "per-primitive sweep sample on host cores (reference modules absent)"},
+        out.update({"value": cb["value"], "ms_per_step": None, "config": head_config(nsm),
+                    "reference_build": "absent: host std::thread port of the same algorithms",
                     "cpu_baseline": cb,
                     "e2e": {"value": cb["value"], "unit": "sync ops/s", "h2d_bytes_per_step": 0,
                             "d2h_bytes_per_step": 0}})
     return out
+
+
+def reference_cells():
+    """The per-cell us/op the reference arm measured on this GPU within the last
+    hour (None when it did not run here)."""
+    try:
+        with open(REF_CELLS_FILE) as f:
+            d = json.load(f)
+    except (OSError, ValueError):
+        return None
+    if d.get("gpu") != gpu_identity() or time.time() - d.get("time", 0) > 3600:
+        return None
+    return d["us_per_op"]
+
+
+def kernel_of(prim):
+    if "Barr" in prim:
+        return "k_barrier"
+    return "k_sem" if "Sem" in prim else "k_mutex"
 
 
 def main():
@@ -514,8 +638,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-check", action="store_true", help="skip the bit-exact check of every run")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-full-sweep", action="store_true", help="skip the 16-primitive sweep beside the headline")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the cluster exchange and mixed-batch figures reported beside the sweep")
+                    help="skip the cluster exchange, batch, serving and UTS figures reported beside the sweep")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -529,9 +654,14 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    flush_buf = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")  # 256 MiB > L2
+
+    def flush():
+        flush_buf.zero_()
+        torch.cuda.synchronize()
 
     if args.impl == "reference":
-        out = reference_arm(args, rank)
+        out = reference_arm(args, rank, flush)
         if rank == 0 and out is not None:
             print(json.dumps(out), flush=True)
         if dist is not None:
@@ -541,15 +671,9 @@ def main():
     import heterosync_gb300 as hs
     nsm = hs.device_info(local)["nsm"] if local == 0 else hs.device_info()["nsm"]
     pts = sweep_points(nsm)
-    flush_buf = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")  # 256 MiB > L2
 
-    def flush():
-        flush_buf.zero_()
-        torch.cuda.synchronize()
-
-    # warm-up: the first W points with a short iteration count
     for s in range(args.warmup):
-        run_step(hs, nsm, pts[s % len(pts)], 20, check=False, flush=flush)
+        run_cells(hs, HEAD_PRIMS, pts[s % len(pts)], WARM_ITERS, check=False, flush=flush)
 
     if dist is not None:
         dist.barrier()
@@ -559,78 +683,86 @@ def main():
     t0 = time.perf_counter()
     recs = []
     for s in range(args.steps):
-        recs += run_step(hs, nsm, pts[s % len(pts)], ITERS, check=not args.no_check, flush=flush)
+        recs += run_cells(hs, HEAD_PRIMS, pts[s % len(pts)], ITERS, check=not args.no_check, flush=flush)
     torch.cuda.synchronize()
     wall_total = time.perf_counter() - t0
     launches = hs.launch_count() - launches0
     ck = clocks.stop()
 
+    cells, value, e2e_value = aggregate(recs)
     ops = sum(r["ops"] for r in recs)
     dev_s = sum(r["ms"] for r in recs) * 1e-3
     e2e_s = sum(r["wall_s"] for r in recs)
     if dist is not None:
-        dev_s, e2e_s, ops = combine_ranks(dist, dev_s, e2e_s, ops, "cuda")
+        # replicas: each rank's sweep rate over the slowest rank's times, all ranks' ops
+        cell_dev_s = sum(c["mean_ms"] for c in cells.values()) * 1e-3
+        cell_e2e_s = sum(c["mean_wall_s"] for c in cells.values())
+        cell_ops = sum(c["ops"] for c in cells.values())
+        mx_dev, mx_e2e, all_ops = combine_ranks(dist, cell_dev_s, cell_e2e_s, cell_ops, "cuda")
+        value, e2e_value = all_ops / mx_dev, all_ops / mx_e2e
+        dev_s, e2e_s, _ = combine_ranks(dist, dev_s, e2e_s, ops, "cuda")
 
     if rank == 0:
-        peak_gbs, peak_kind = load_peaks()
-        # dominant kernel: the (primitive) with the largest share of device time
-        by_prim = {}
-        for r in recs:
-            d = by_prim.setdefault(r["prim"], {"ops": 0, "ms": 0.0, "bytes": 0, "launches": 0})
-            d["ops"] += r["ops"]
-            d["ms"] += r["ms"]
-            d["bytes"] += cs_bytes(r["prim"], r["num_tbs"], r["num_ldst"], nsm)
-            d["launches"] += 1
-        dom = max(by_prim, key=lambda k: by_prim[k]["ms"])
-        dd = by_prim[dom]
-        achieved = dd["bytes"] / (dd["ms"] * 1e-3) / 1e9
-        atom_peak, same_rate = l2_atomic_peak(hs)
-        try:
-            lock_latency_out = lock_latency(hs, recs, nsm)
-        except Exception as e:  # noqa: BLE001
-            lock_latency_out = {"error": str(e)}
-        atom_achieved = sum(by_prim[k]["ops"] * ATOMICS_PER_OP[k] for k in by_prim) / dev_s
-        sub = [r for r in recs if r["prim"] in REF_PRIMS]
-        sub_ops = sum(r["ops"] for r in sub)
-        same_subset = {"primitives": REF_PRIMS, "value": sub_ops / (sum(r["ms"] for r in sub) * 1e-3),
-                       "e2e": sub_ops / sum(r["wall_s"] for r in sub), "unit": "sync ops/s",
-                       "note": "the mutex and barrier cells only: the reference arm's workload"}
+        by_kernel = {}
+        for c in cells.values():
+            by_kernel[kernel_of(c["prim"])] = by_kernel.get(kernel_of(c["prim"]), 0.0) + c["mean_ms"]
+        mutexes = [p for p in HEAD_PRIMS if p in LOCK_CHAIN]
+        floors, lat = lock_floors(hs, SWEEP_PRIMS)
+        roofline = latency_roofline(cells, floors, mutexes, DRAM_BYTES_PER_LAUNCH)
+        roofline["share_of_device_time"] = by_kernel.get("k_mutex", 0.0) / sum(by_kernel.values())
         out = {
-            "metric": "sync ops/s", "value": ops / dev_s, "unit": "sync ops/s", "n_gpus": world,
+            "metric": "sync ops/s", "value": value, "unit": "sync ops/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
             "data": "synthetic (seeded uint32 shared data, bit-exact final state checked every run)",
-            "config": {"workload": "per-primitive sweep: 16 SyncPrims x numTBs {%s} x numLdSt {10,100}, "
-                                   "256 threads/TB, 1000 CS iterations, reference critical section"
-                                   % ",".join(str(m * nsm) for m in TB_MULT),
-                       "threads": THREADS, "num_iters": ITERS, "num_ldst": list(LDST),
-                       "num_tbs": [m * nsm for m in TB_MULT], "primitives": SWEEP_PRIMS,
-                       "step": "one launch of each primitive at one (numTBs, numLdSt) point; steps cycle the "
-                               "6 points", "l2": "flushed before every run (256 MiB write)",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
-            "e2e": {"value": ops / e2e_s, "unit": "sync ops/s",
+            "config": head_config(nsm),
+            "e2e": {"value": e2e_value, "unit": "sync ops/s",
                     "h2d_bytes_per_step": int(sum(r["bytes"] for r in recs) / args.steps),
                     "d2h_bytes_per_step": int(sum(r["bytes"] for r in recs) / args.steps)},
             "gpu_launches": launches,
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
-                         "frac": achieved / peak_gbs, "peak_source": peak_kind, "traffic": DRAM_BYTES_PER_LAUNCH,
-                         "traffic_source": TRAFFIC_SOURCE,
-                         "note": "critical-section bytes; these kernels are latency-bound (lock hand-off), see "
-                                 "l2_atomic"},
-            "l2_atomic": {"achieved": atom_achieved, "peak": atom_peak,
-                          "frac": (atom_achieved / atom_peak) if atom_peak else None, "unit": "atomics/s",
-                          "same_address_rate": same_rate,
-                          "note": "peak: contention-free red.add probe; same_address_rate: one word"},
-            "lock_latency": lock_latency_out,
-            "same_subset": same_subset,
-            "per_prim": {k: {"ops_per_s": v["ops"] / (v["ms"] * 1e-3), "ms": round(v["ms"], 3)}
-                         for k, v in by_prim.items()},
-            "per_point_us_per_op": {"%s@%d/%d" % (r["prim"], r["num_tbs"], r["num_ldst"]):
-                                    round(r["ms"] * 1e3 / r["ops"], 3) for r in recs},
+            "roofline": roofline,
+            "secondary_bounds": secondary_bounds(hs, cells, nsm, sum(c["mean_ms"] for c in cells.values()) * 1e-3),
+            "lock_latency": lat,
+            "kernel_share": {k: round(v / sum(by_kernel.values()), 4) for k, v in by_kernel.items()},
+            "per_prim": {p: {"ops_per_s": sum(c["ops"] for c in cells.values() if c["prim"] == p) /
+                             (sum(c["mean_ms"] for c in cells.values() if c["prim"] == p) * 1e-3)}
+                         for p in HEAD_PRIMS if any(c["prim"] == p for c in cells.values())},
+            "per_cell_us_per_op": {k: round(c["us_per_op"], 4) for k, c in cells.items()},
+            "parallelism": "replicas" if world > 1 else "single GPU",
             "wall_s": wall_total,
         }
+        ref = reference_cells()
+        if ref:
+            cmp = {k: round(ref[k] / c["us_per_op"], 3) for k, c in cells.items() if k in ref}
+            out["per_cell_vs_reference"] = {"speedup": cmp, "min": min(cmp.values()) if cmp else None,
+                                            "source": "the reference arm's per-cell us/op on this GPU, run just "
+                                                      "before (reference us/op / this build's us/op)"}
         if ck:
             out["clocks"] = ck
+        if not args.no_full_sweep and world == 1:
+            srecs = []
+            for pt in pts:
+                srecs += run_cells(hs, SEM_PRIMS, pt, ITERS, check=not args.no_check, flush=flush)
+            scells, _, _ = aggregate(srecs)
+            allc = dict(cells)
+            allc.update(scells)
+            fops = sum(c["ops"] for c in allc.values())
+            fms = sum(c["mean_ms"] for c in allc.values())
+            fwall = sum(c["mean_wall_s"] for c in allc.values())
+            sk = {}
+            for c in allc.values():
+                sk[kernel_of(c["prim"])] = sk.get(kernel_of(c["prim"]), 0.0) + c["mean_ms"]
+            sem_roof = latency_roofline(scells, floors, SEM_PRIMS, None)
+            sem_roof["kernel"] = "k_sem"
+            sem_roof["traffic_source"] = None
+            out["full_sweep"] = {
+                "workload": "16 SyncPrims (the headline 8 plus spinSem{1,2,10,120}, spinSemEBO{1,2,10,120}) x the "
+                            "same 6 points, numCSIters 1000; semaphore cells run once each after the timed steps",
+                "value": fops / (fms * 1e-3), "e2e": fops / fwall, "unit": "sync ops/s",
+                "kernel_share": {k: round(v / fms, 4) for k, v in sk.items()},
+                "roofline": sem_roof,
+                "per_cell_us_per_op": {k: round(c["us_per_op"], 4) for k, c in scells.items()},
+                "note": "the reference's semaphore kernels cannot run on GB300: " + REF_EXCLUDED}
         if not args.no_extras and world == 1:
             for key, fn in (("fa_mutex_slice", lambda h: fa_mutex_slice_extra(h, nsm)), ("exchange", exchange_extra),
                             ("batch", batch_extra), ("serve", serve_extra), ("uts_geo", uts_geo_extra)):

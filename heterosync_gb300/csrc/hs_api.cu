@@ -16,6 +16,7 @@ namespace hs {
 using KernelFn = void (*)(RunDesc);
 KernelFn syncprim_plan(int prim, int mode, int threads, int num_ldst, size_t* smem_bytes, bool bulk = true);
 cudaError_t prepare_smem(KernelFn fn, size_t smem_bytes);
+size_t barrier_tile_bytes(int threads, int num_ldst, int num_tbs, int phys_nsm, size_t base);
 KernelFn prim_cluster_kernel(int mode);
 cudaError_t launch_ring_init(unsigned* ring, unsigned slots_per_group, unsigned groups, cudaStream_t st);
 cudaError_t launch_fill_lines(unsigned* base, size_t n, size_t stride, unsigned value, cudaStream_t st);
@@ -542,16 +543,8 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c0, void* storage, int o
   size_t smem = 0;
   KernelFn fn = syncprim_plan(c->prim, c->mode, c->threads, c->num_ldst, &smem, !(c->flags & HS_RUN_REGISTER_CS));
   if (!fn) { g_err = "no kernel for this primitive/mode"; return r->status = HS_EINVAL; }
-  if (is_barrier(c->prim) && smem > 0) {
-    // bulk-copy tiles: the shared memory the co-resident TBs of one SM leave
-    // free (one TB per SM takes a whole chunk, four take 48 KB tiles)
-    const size_t chunk = (size_t)c->threads * (c->num_ldst + 1) * 4;
-    const size_t region = (size_t)64 * (c->num_ldst + 1);
-    const int per_sm = (c->num_tbs + ctx->nsm - 1) / ctx->nsm;
-    size_t budget = per_sm > 0 ? (size_t)(216 * 1024) / (size_t)per_sm : smem;
-    budget = std::min(budget, (size_t)(200 * 1024)) / region * region;  // the bulk-copy path's cap
-    smem = std::max(smem, std::min(chunk, budget));
-  }
+  // bulk-copy tiles of a barrier: the shared memory its co-resident TBs leave free
+  if (is_barrier(c->prim)) smem = barrier_tile_bytes(c->threads, c->num_ldst, c->num_tbs, ctx->nsm, smem);
   HS_CK(prepare_smem(fn, smem));
   // Tree barriers whose logical-SM groups are all the same size (numTBs a
   // multiple of NUM_SM, 2 to 8 per group) run each group as one thread-block
@@ -669,9 +662,10 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c0, void* storage, int o
   d.cluster = cluster;
   d.variant = variant;
   r->cluster = cluster;
-  // global spin / FA mutex with more than one TB: the die-aware cohort lock
-  if ((c->prim == 4 || c->prim == 7) && c->num_tbs > 1 && grid == c->num_tbs && !(c->flags & HS_RUN_NO_COHORT) &&
-      cohort_ready(ctx)) {
+  // global spin / FA mutex, or global semaphore (its writers), with more than
+  // one TB: the die-aware cohort form
+  if ((c->prim == 4 || c->prim == 7 || (c->prim >= 8 && c->prim <= 15)) && c->num_tbs > 1 && grid == c->num_tbs &&
+      !(c->flags & HS_RUN_NO_COHORT) && cohort_ready(ctx)) {
     d.cohort = 1;
     d.die_map = reinterpret_cast<const unsigned char*>(ctx->coh_pool);
     for (int i = 0; i < 6; ++i) {

@@ -34,6 +34,7 @@ namespace hs {
 using KernelFn = void (*)(RunDesc);
 KernelFn syncprim_plan(int prim, int mode, int threads, int num_ldst, size_t* smem_bytes, bool bulk = true);
 cudaError_t prepare_smem(KernelFn fn, size_t smem_bytes);
+size_t barrier_tile_bytes(int threads, int num_ldst, int num_tbs, int phys_nsm, size_t base);
 cudaError_t launch_ring_init(unsigned* ring, unsigned slots_per_group, unsigned groups, cudaStream_t st);
 cudaError_t launch_fill_lines(unsigned* base, size_t n, size_t stride, unsigned value, cudaStream_t st);
 }  // namespace hs
@@ -51,19 +52,31 @@ thread_local char g_noalloc_err[256];  // fixed buffer: the error path allocates
 
 void set_err(const char* msg) { std::snprintf(g_noalloc_err, sizeof(g_noalloc_err), "%s", msg); }
 
+// A failed CUDA call: its text goes to the error buffer, and a non-sticky error
+// is cleared from the runtime so it cannot surface in an unrelated later call.
+int cuda_err(cudaError_t e, const char* what) {
+  std::snprintf(g_noalloc_err, sizeof(g_noalloc_err), "%s: %s", what, cudaGetErrorString(e));
+  cudaGetLastError();
+  return HS_ECUDA;
+}
+#define NA_CK(call)                                          \
+  do {                                                       \
+    cudaError_t e_ = (call);                                 \
+    if (e_ != cudaSuccess) return r->status = cuda_err(e_, #call); \
+  } while (0)
+
 // Device address of the scratch array on the current device (looked up once per device).
 int scratch_address(unsigned** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return HS_ECUDA;
-  if (dev < 0 || dev >= kMaxDevices) return HS_EINVAL;
+  if (e != cudaSuccess) return cuda_err(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) { set_err("device index beyond the scratch table"); return HS_EINVAL; }
   std::lock_guard<std::mutex> lk(g_mu);
   if (!g_addr[dev]) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, hs_noalloc_scratch);
     if (e != cudaSuccess || !p) {
-      std::snprintf(g_noalloc_err, sizeof(g_noalloc_err), "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-      return HS_ECUDA;
+      return cuda_err(e != cudaSuccess ? e : cudaErrorInvalidSymbol, "cudaGetSymbolAddress");
     }
     g_addr[dev] = static_cast<unsigned*>(p);
   }
@@ -87,20 +100,34 @@ extern "C" int hs_run_noalloc(const hs_run_config* c0, void* storage, void* stre
   const hs_run_config* c = &cc;
   std::memset(r, 0, sizeof(*r));
   r->cluster = 1;
-  int dev = 0, nsm = c->nsm;
-  if (cudaGetDevice(&dev) != cudaSuccess) return r->status = HS_ECUDA;
-  if (nsm <= 0 && cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-    return r->status = HS_ECUDA;
+  // Runs here are always the flat, single-CTA-per-TB form with the plain (not
+  // die-aware) locks and fresh lock state: the flags that ask for that, or for
+  // host synchronisation after each launch, are honoured; the others would need
+  // state or launches this entry point does not have and are refused.
+  const int kHonoured = HS_RUN_SYNC_EACH | HS_RUN_NO_CLUSTER | HS_RUN_REGISTER_CS | HS_RUN_NO_COHORT;
+  if (c->flags & ~kHonoured) {
+    set_err("hs_run_noalloc takes only HS_RUN_SYNC_EACH, HS_RUN_NO_CLUSTER, HS_RUN_REGISTER_CS and "
+            "HS_RUN_NO_COHORT (no kept state, graphs or cluster critical sections)");
+    return r->status = HS_EINVAL;
+  }
+  int dev = 0, dev_sms = 0;
+  NA_CK(cudaGetDevice(&dev));
+  NA_CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, dev));
+  const int nsm = c->nsm > 0 ? c->nsm : dev_sms;
   size_t words = 0;
   int s = hs_storage_words(c, nsm, &words);
   if (s) { set_err(hs_last_error()); return r->status = s; }
   size_t smem = 0;
-  KernelFn fn = syncprim_plan(c->prim, c->mode, c->threads, c->num_ldst, &smem);
+  KernelFn fn = syncprim_plan(c->prim, c->mode, c->threads, c->num_ldst, &smem, !(c->flags & HS_RUN_REGISTER_CS));
   if (!fn) { set_err("no kernel for this primitive/mode"); return r->status = HS_EINVAL; }
-  if (prepare_smem(fn, smem) != cudaSuccess) return r->status = HS_ECUDA;
+  const bool barrier = c->prim >= 0 && c->prim <= 3;
+  // a barrier's bulk-copy tiles: the same size hs_run() gives them
+  if (barrier) smem = barrier_tile_bytes(c->threads, c->num_ldst, c->num_tbs, dev_sms, smem);
+  NA_CK(prepare_smem(fn, smem));
 
   Layout lay;
-  hs_layout_for(c, nsm, &lay);
+  std::memset(&lay, 0, sizeof(lay));
+  if ((s = hs_layout_for(c, nsm, &lay))) { set_err("no lock-state layout for this run"); return r->status = s; }
   const size_t w_status = 64;
   const size_t w_locks = round64((size_t)lay.lines * kLineWords);
   const size_t w_ring = round64(lay.ring_words);
@@ -113,15 +140,14 @@ extern "C" int hs_run_noalloc(const hs_run_config* c0, void* storage, void* stre
     return r->status = HS_EINVAL;
   }
   int max_tpb = 0;
-  if (cudaDeviceGetAttribute(&max_tpb, cudaDevAttrMaxThreadsPerBlock, dev) != cudaSuccess) return r->status = HS_ECUDA;
+  NA_CK(cudaDeviceGetAttribute(&max_tpb, cudaDevAttrMaxThreadsPerBlock, dev));
   if (c->threads > max_tpb) { set_err("threads per TB above the device limit"); return r->status = HS_EINVAL; }
-  if (c->prim >= 0 && c->prim <= 3) {
-    int per_sm = 0, dev_sms = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, c->threads, 0) != cudaSuccess ||
-        cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-      return r->status = HS_ECUDA;
+  if (barrier) {  // every TB of a barrier must be resident at once, with the shared memory it launches with
+    int per_sm = 0;
+    NA_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, c->threads, smem));
     if ((long long)per_sm * dev_sms < c->num_tbs) {
-      set_err("barrier TBs cannot all be co-resident");
+      std::snprintf(g_noalloc_err, sizeof(g_noalloc_err),
+                    "barrier TBs cannot all be co-resident (%d per SM x %d SMs < %d)", per_sm, dev_sms, c->num_tbs);
       return r->status = HS_ENORES;
     }
   }
@@ -160,36 +186,41 @@ extern "C" int hs_run_noalloc(const hs_run_config* c0, void* storage, void* stre
 
   const auto t0 = std::chrono::steady_clock::now();
   // clear what must start at zero: status and lock state (the array keeps the last call's contents)
-  if (cudaMemsetAsync(d.status, 0, w_status * 4, st) != cudaSuccess) return r->status = HS_ECUDA;
-  if (cudaMemsetAsync(d.locks, 0, w_locks * 4, st) != cudaSuccess) return r->status = HS_ECUDA;
+  NA_CK(cudaMemsetAsync(d.status, 0, w_status * 4, st));
+  NA_CK(cudaMemsetAsync(d.locks, 0, w_locks * 4, st));
   unsigned extra = 0;
   if (hs_prim_sem_count(c->prim)) {
-    if (launch_fill_lines(d.locks + (size_t)lay.l_grp * kLineWords, (size_t)lay.groups, (size_t)4 * kLineWords,
-                          d.sem_max, st) != cudaSuccess)
-      return r->status = HS_ECUDA;
+    NA_CK(launch_fill_lines(d.locks + (size_t)lay.l_grp * kLineWords, (size_t)lay.groups, (size_t)4 * kLineWords,
+                            d.sem_max, st));
     ++extra;
   }
   if (c->prim == 6 || c->prim == 22) {
-    if (launch_ring_init(d.ring, d.ring_max + 1u, c->prim == 22 ? (unsigned)nsm : 1u, st) != cudaSuccess)
-      return r->status = HS_ECUDA;
+    NA_CK(launch_ring_init(d.ring, d.ring_max + 1u, c->prim == 22 ? (unsigned)nsm : 1u, st));
     ++extra;
   }
   for (int rep = 0; rep < c->repeats; ++rep) {
     void* args[] = {&d};
-    if (cudaLaunchKernel((const void*)fn, dim3(c->num_tbs), dim3(c->threads), args, smem, st) != cudaSuccess)
-      return r->status = HS_ECUDA;
+    NA_CK(cudaLaunchKernel((const void*)fn, dim3(c->num_tbs), dim3(c->threads), args, smem, st));
     r->launches++;
+    if (c->flags & HS_RUN_SYNC_EACH) NA_CK(cudaStreamSynchronize(st));
   }
   hs_note_launches(r->launches + extra);
   unsigned h[2] = {0, 0};
-  if (cudaMemcpyAsync(h, d.status, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess) return r->status = HS_ECUDA;
-  if (cudaStreamSynchronize(st) != cudaSuccess) return r->status = HS_ECUDA;
+  NA_CK(cudaMemcpyAsync(h, d.status, sizeof(h), cudaMemcpyDeviceToHost, st));
+  NA_CK(cudaStreamSynchronize(st));
   r->elapsed_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
   r->avg_ms = c->repeats ? r->elapsed_ms / c->repeats : 0.f;
   r->ops = (unsigned long long)c->num_tbs * c->num_iters * c->repeats;
   r->dev_error_bits = h[0];
   r->dev_error_site = h[1];
-  if (h[0] & HS_DEV_TIMEOUT) { set_err("device wait timed out"); return r->status = HS_ETIMEDOUT; }
-  if (h[0]) { set_err("device error"); return r->status = HS_EMISMATCH; }
+  if (h[0] & HS_DEV_TIMEOUT) {
+    std::snprintf(g_noalloc_err, sizeof(g_noalloc_err), "device wait timed out at site %u", h[1]);
+    return r->status = HS_ETIMEDOUT;
+  }
+  if (h[0]) {
+    std::snprintf(g_noalloc_err, sizeof(g_noalloc_err), "device error bits %u", h[0]);
+    return r->status = HS_EMISMATCH;
+  }
+  g_noalloc_err[0] = '\0';
   return r->status = HS_OK;
 }

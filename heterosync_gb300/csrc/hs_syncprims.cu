@@ -17,6 +17,7 @@
 //  * barrier state is generation-valued (no resets) and groups may be uneven;
 //  * every wait is bounded (see hs_device.cuh).
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cstdlib>
 #include "hs_exec.cuh"
 
@@ -127,13 +128,25 @@ __global__ void __launch_bounds__(TMA ? 256 : Bounds<V>::kThreads) k_mutex(RunDe
                                       tma, env);
 }
 
-// One TB's iterations of a semaphore kernel, at scope S.
+// One TB's iterations of a semaphore kernel, at scope S.  A global semaphore
+// with d.cohort set runs its writers as die cohorts (cohort_sem_writer_wait).
 template <int S, bool EBO, bool UNIQ, int MODE, int V, bool TMA>
 __device__ __forceinline__ void sem_loop(const RunDesc& d, int b, int numSM, int k, bool writer, unsigned* st,
                                          int rchunk, TmaCtx& tma, const HsEnv& env) {
   const int Gd = d.num_tbs;
+  unsigned* local = nullptr;  // the writer's die cohort word (cohort runs only)
+  if constexpr (S == GPU && !UNIQ) {
+    if (d.cohort && writer) {
+      unsigned sm;
+      asm volatile("mov.u32 %0, %%smid;" : "=r"(sm));
+      local = d.coh[3 * (d.die_map[sm & 255u] & 1)];
+    }
+  }
   for (int i = 0; i < d.iters; ++i) {
-    if (!sem_wait<S>(st, writer, d.sem_max, EBO, !UNIQ, d.bo_min, d.bo_max, env)) break;
+    unsigned pc = 0, others = 0;  // cohort state (master thread)
+    const bool got = local ? cohort_sem_writer_wait(local, st, d.sem_max, EBO, d.bo_min, d.bo_max, env, pc, others)
+                           : sem_wait<S>(st, writer, d.sem_max, EBO, !UNIQ, d.bo_min, d.bo_max, env);
+    if (!got) break;
     bool ok = true;
     if (writer) {
       int cur = UNIQ ? b : 0;
@@ -146,7 +159,8 @@ __device__ __forceinline__ void sem_loop(const RunDesc& d, int b, int numSM, int
       if constexpr (TMA) ok = cs_read_tma(d, rchunk, tma, env, d.sink + b);
       else cs_read(d.data + (size_t)rchunk * chunk_words(d.T, d.L), d.T, d.L, d.sink + b);
     }
-    sem_post<S>(st, writer, d.sem_max);
+    if (local) cohort_sem_writer_post(local, st, d.sem_max, pc, others);
+    else sem_post<S>(st, writer, d.sem_max);
     if (!ok) break;
   }
 }
@@ -531,6 +545,20 @@ KernelFn syncprim_plan(int prim, int mode, int threads, int num_ldst, size_t* sm
   }
   if (threads > 512) return pick_v<4, false>(prim, mode);
   return pick_v<8, false>(prim, mode);
+}
+
+// Dynamic shared memory of a barrier launch whose plan took the bulk-copy path
+// (base > 0): the shared memory the co-resident TBs of one SM leave free, so one
+// TB per SM stages a whole chunk and four take 48 KB tiles (whole half-warp
+// regions, at most the bulk-copy path's cap).  phys_nsm is the device's SM count.
+size_t barrier_tile_bytes(int threads, int num_ldst, int num_tbs, int phys_nsm, size_t base) {
+  if (base == 0 || phys_nsm <= 0) return base;
+  const size_t chunk = (size_t)threads * (num_ldst + 1) * 4;
+  const size_t region = (size_t)64 * (num_ldst + 1);
+  const int per_sm = (num_tbs + phys_nsm - 1) / phys_nsm;
+  size_t budget = per_sm > 0 ? (size_t)(216 * 1024) / (size_t)per_sm : base;
+  budget = std::min(budget, (size_t)kTmaMaxBytes) / region * region;
+  return std::max(base, std::min(chunk, budget));
 }
 
 KernelFn syncprim_kernel(int prim, int mode, int threads, int num_ldst) {

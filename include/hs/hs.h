@@ -50,8 +50,9 @@ enum {
   HS_RUN_REGISTER_CS = 8, /* critical sections on the register path only (no bulk copies through shared memory) */
   HS_RUN_GRAPH = 16,      /* the repeats as one CUDA graph: captured once per context and launch shape, then
                              replayed (not with HS_RUN_SYNC_EACH); the lock state is still reset before it */
-  HS_RUN_NO_COHORT = 32,  /* global spin / FA mutexes: one lock word for the whole GPU instead of the
-                             die-aware cohort (a lock per die, homed on it, handed on within the die) */
+  HS_RUN_NO_COHORT = 32,  /* global spin / FA mutexes and global semaphores' writers: one lock word for the
+                             whole GPU instead of the die-aware cohort (a lock per die, homed on it, handed
+                             on within the die) */
   HS_RUN_CLUSTER_CS = 64  /* global mutexes and semaphores with numLdSt > 32: one thread-block cluster per
                              logical TB, the critical section split over its SMs, for every such run (by
                              default only semaphores whose writers own 4 or more chunks, where it is faster) */
@@ -86,7 +87,7 @@ typedef struct hs_run_result {
   unsigned long long ops;       /* num_tbs * num_iters * repeats */
   unsigned launches;            /* kernels launched by this call */
   int cluster;                  /* tree barriers: CTAs per thread-block cluster (1: no clusters) */
-  int cohort;                   /* global mutexes: 1 if the die-aware cohort lock ran */
+  int cohort;                   /* global mutexes and semaphores: 1 if the die-aware cohort form ran */
 } hs_run_result;
 
 typedef struct hs_ctx hs_ctx;
@@ -144,7 +145,13 @@ int hs_expected_storage(const hs_run_config* cfg, int nsm, const uint32_t* init,
  * device memory.  The first call on a device looks up the array's address:
  * make it before any stream capture.  All calls share the array, so calls that
  * overlap on the GPU race; each call clears the state it needs.  elapsed_ms is
- * host wall time around the launches (no events are created). */
+ * host wall time around the launches (no events are created).  Runs are always
+ * the flat form (one CTA per TB, no clusters, plain rather than die-aware
+ * locks, fresh lock state): cfg->flags may hold HS_RUN_SYNC_EACH,
+ * HS_RUN_NO_CLUSTER, HS_RUN_REGISTER_CS and HS_RUN_NO_COHORT, and any other
+ * flag is rejected with HS_EINVAL.  Barriers whose TBs cannot all be resident
+ * with the shared memory they launch with are rejected with HS_ENORES before
+ * anything is launched. */
 #define HS_NOALLOC_SCRATCH_BYTES (1u << 20)
 int hs_run_noalloc(const hs_run_config* cfg, void* storage, void* stream, hs_run_result* result);
 const char* hs_noalloc_last_error(void);

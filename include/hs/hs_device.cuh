@@ -432,6 +432,72 @@ __device__ __forceinline__ bool sem_wait(unsigned* st, bool writer, unsigned max
   }
   return __syncthreads_or(ok) != 0;
 }
+// Die-aware (cohort) writers of a global semaphore.  Writers exclude one
+// another and every reader, so, like the cohort mutexes, the writers of one die
+// form a cohort with a local word homed on that die (the cohort_tas_lock
+// encoding: [31:16] waiters, [15:1] passes so far, [0] held).  A writer that
+// takes the local word without inheriting (passes == 0) takes the semaphore by
+// the reference's writer rule (count == maxc, else set writer-waiting); on
+// release, a writer with a waiter on its die passes the semaphore to it (at
+// most kCohortMaxPass times in a row) instead of posting, otherwise it posts
+// (count += maxc) and frees the local word.  A pass is what the reference's
+// rules would give as well: a waiting writer has writer-waiting set, so no
+// reader can enter between the post and that writer's acquisition; here the
+// count simply stays 0 across it.  The hand-off between two writers of a die
+// then touches only a line homed on that die, and only one writer per die
+// polls the semaphore word.
+__device__ __forceinline__ bool cohort_sem_writer_wait(unsigned* local, unsigned* st, unsigned maxc, bool ebo,
+                                                       unsigned bmin, unsigned bmax, const HsEnv& env, unsigned& pc,
+                                                       unsigned& others) {
+  int ok = 0;
+  if (is_master()) {
+    unsigned b = bmin;
+    auto backoff = [&] {
+      if (ebo) {
+        sleep_ns(b);
+        b = ebo_next(b, bmax);
+      }
+    };
+    atomicAdd(local, 1u << 16);  // register as a waiter
+    unsigned got = 0;
+    ok = wait_until_p(
+        [&] {
+          const unsigned v = ld_relaxed<GPU>(local);
+          if (v & 1u) return false;
+          if (atom_cas_acquire<GPU>(local, v, (v | 1u) - (1u << 16)) != v) return false;
+          got = v;
+          return true;
+        },
+        [&] { return ld_relaxed<GPU>(local); }, backoff, env, HS_SITE_SEM_WAIT);
+    pc = (got >> 1) & 0x7FFFu;
+    others = (got >> 16) - 1u;
+    if (ok && pc == 0u) {  // the cohort does not hold the semaphore: take it by the writer rule
+      b = bmin;
+      ok = wait_until_p(
+          [&] {
+            const unsigned s = ld_relaxed<GPU>(st);
+            if ((s & kSemCnt) == maxc) return atom_cas_acquire<GPU>(st, s, 0u) == s;
+            if (!(s & kSemWW)) atom_or_relaxed<GPU>(st, kSemWW);
+            return false;
+          },
+          [&] { return ld_relaxed<GPU>(st); }, backoff, env, HS_SITE_SEM_WAIT);
+    }
+  }
+  return __syncthreads_or(ok) != 0;
+}
+__device__ __forceinline__ void cohort_sem_writer_post(unsigned* local, unsigned* st, unsigned maxc, unsigned pc,
+                                                       unsigned others) {
+  __syncthreads();  // every thread's critical-section stores precede the release
+  if (is_master()) {
+    if (others != 0u && pc + 1u < kCohortMaxPass) {
+      red_release_add<GPU>(local, 1u);  // pass the semaphore to a writer of this die
+    } else {
+      red_release_add<GPU>(st, maxc);
+      red_release_add<GPU>(local, 0u - (2u * pc + 1u));
+    }
+  }
+}
+
 template <int S>
 __device__ __forceinline__ void sem_post(unsigned* st, bool writer, unsigned maxc) {
   __syncthreads();

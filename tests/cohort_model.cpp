@@ -1,12 +1,16 @@
-// Host model of the cohort (die-aware) mutex protocols of include/hs/hs_device.cuh
-// (cohort_tas_lock / cohort_tas_unlock, cohort_ticket_lock / cohort_ticket_unlock),
-// run by std::threads standing for TBs, split over two "dies".  The encodings
-// are the device code's; the ticket wraps and the pass limit are parameters,
-// so that small values drive the wrap-around and global-release branches often.
-// Checks: mutual exclusion (a non-atomic counter and an owner word inside the
-// critical section) and the final state of every lock word.  Test code only.
+// Host model of the cohort (die-aware) protocols of include/hs/hs_device.cuh
+// (cohort_tas_lock / cohort_tas_unlock, cohort_ticket_lock / cohort_ticket_unlock,
+// and the semaphore's cohort writers, cohort_sem_writer_wait / _post, beside
+// readers that follow sem_try_once's reader rule), run by std::threads standing
+// for TBs, split over two "dies".  The encodings are the device code's; the
+// ticket wraps and the pass limit are parameters, so that small values drive
+// the wrap-around and global-release branches often.  Checks: mutual exclusion
+// (a non-atomic counter and an owner word inside the critical section; for the
+// semaphore, no reader beside a writer and at most N readers at once) and the
+// final state of every lock word.  Test code only.
 //
 //   cohort_model tas|ticket <threads> <iters> <max_pass> <local_wrap> <global_wrap>
+//   cohort_model sem <threads> <iters> <max_pass> <readers> <N>
 // prints "ok <counter>" or "FAIL <reason>" and exits 0 / 1.
 #include <atomic>
 #include <cstdint>
@@ -103,15 +107,94 @@ void ticket_thread(int me, int die, int iters) {
   }
 }
 
+// --- semaphore: one word, [30:0] count (starts at maxc = N + 1), [31] writer-waiting
+constexpr u32 kWW = 0x80000000u, kCnt = 0x7FFFFFFFu;
+std::atomic<u32> sem{0};
+std::atomic<int> writers_in{0}, readers_in{0};
+std::atomic<unsigned long long> reader_ops{0};
+u32 kMaxc = 2;
+
+void sem_writer_thread(int me, int die, int iters) {
+  std::atomic<u32>& local = l_word[die];
+  for (int i = 0; i < iters; ++i) {
+    local.fetch_add(1u << 16, std::memory_order_relaxed);
+    u32 got;
+    for (;;) {
+      u32 v = local.load(std::memory_order_relaxed);
+      if (v & 1u) continue;
+      if (local.compare_exchange_weak(v, (v | 1u) - (1u << 16), std::memory_order_acquire)) {
+        got = v;
+        break;
+      }
+    }
+    const u32 pc = (got >> 1) & 0x7FFFu, others = (got >> 16) - 1u;
+    if (pc == 0u) {  // take the semaphore by the writer rule
+      for (;;) {
+        u32 s = sem.load(std::memory_order_relaxed);
+        if ((s & kCnt) == kMaxc) {
+          if (sem.compare_exchange_strong(s, 0u, std::memory_order_acquire)) break;
+          continue;
+        }
+        if (!(s & kWW)) sem.fetch_or(kWW, std::memory_order_relaxed);
+      }
+    }
+    if (writers_in.fetch_add(1) != 0 || readers_in.load() != 0) bad = true;
+    critical_section(me);
+    if (readers_in.load() != 0 || writers_in.fetch_sub(1) != 1) bad = true;
+    if (others != 0u && pc + 1u < kMaxPass) {
+      local.fetch_add(1u, std::memory_order_release);
+    } else {
+      sem.fetch_add(kMaxc, std::memory_order_release);
+      local.fetch_add(0u - (2u * pc + 1u), std::memory_order_release);
+    }
+  }
+}
+
+void sem_reader_thread(int, int, int iters) {
+  for (int i = 0; i < iters; ++i) {
+    for (;;) {
+      u32 s = sem.load(std::memory_order_relaxed);
+      if (!(s & kWW) && (s & kCnt) > 1u && sem.compare_exchange_strong(s, s - 1u, std::memory_order_acquire)) break;
+    }
+    const int r = readers_in.fetch_add(1);
+    if (r >= (int)kMaxc - 1 || writers_in.load() != 0) bad = true;
+    reader_ops.fetch_add(1);
+    readers_in.fetch_sub(1);
+    sem.fetch_add(1u, std::memory_order_release);
+  }
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
   if (argc != 7) {
-    std::fprintf(stderr, "usage: cohort_model tas|ticket threads iters max_pass local_wrap global_wrap\n");
+    std::fprintf(stderr, "usage: cohort_model tas|ticket threads iters max_pass local_wrap global_wrap\n"
+                         "       cohort_model sem threads iters max_pass readers N\n");
     return 2;
   }
   const bool tas = std::strcmp(argv[1], "tas") == 0;
   const int n = std::atoi(argv[2]), iters = std::atoi(argv[3]);
+  if (std::strcmp(argv[1], "sem") == 0) {
+    kMaxPass = (u32)std::atoi(argv[4]);
+    const int readers = std::atoi(argv[5]);
+    kMaxc = (u32)std::atoi(argv[6]) + 1u;
+    sem = kMaxc;
+    l_word[0] = 0;
+    l_word[1] = 0;
+    std::vector<std::thread> ts;
+    for (int t = 0; t < n; ++t) ts.emplace_back(sem_writer_thread, t, t % 2, iters);
+    for (int t = 0; t < readers; ++t) ts.emplace_back(sem_reader_thread, n + t, 0, iters);
+    for (auto& t : ts) t.join();
+    const unsigned long long want = (unsigned long long)n * (unsigned long long)iters;
+    if (bad.load()) return std::puts("FAIL a reader beside a writer, two writers, or too many readers"), 1;
+    if (counter != want) return std::printf("FAIL counter %llu of %llu\n", counter, want), 1;
+    if (reader_ops.load() != (unsigned long long)readers * iters) return std::puts("FAIL reader count"), 1;
+    if (sem.load() != kMaxc) return std::printf("FAIL semaphore word %#x at the end\n", sem.load()), 1;
+    for (int d = 0; d < 2; ++d)
+      if (l_word[d].load() != 0u) return std::printf("FAIL local word %d = %#x at the end\n", d, l_word[d].load()), 1;
+    std::printf("ok %llu\n", counter);
+    return 0;
+  }
   kMaxPass = (u32)std::atoi(argv[4]);
   kLocalWrap = (u32)std::strtoul(argv[5], nullptr, 10);
   kGlobalWrap = (u32)std::strtoul(argv[6], nullptr, 10);

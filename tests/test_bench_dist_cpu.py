@@ -30,7 +30,7 @@ def _worker(rank, world, port, out):
 
     class Args:
         gpus, steps, warmup = world, 1, 3
-    ref = bench.reference_arm(Args, rank) if rank != 0 else "rank0"
+    ref = bench.reference_arm(Args, rank, None) if rank != 0 else "rank0"
     out[rank] = (dev_s, e2e_s, ops, ref)
     dist.destroy_process_group()
 

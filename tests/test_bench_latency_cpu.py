@@ -1,7 +1,9 @@
-"""bench.py's lock-latency floors, from a stand-in probe and sweep records (no
-GPU): a CAS lock's floor is hand-off + atomic + 2 x L2 load, a queue lock's
-drops the atomic; each numLdSt-10 lock cell at NUM_SM TBs is reported as the
-fraction of its floor; other cells are left out."""
+"""bench.py's latency roofline, from stand-ins for the probe and the runs (no
+GPU): a lock's floor per op is one hand-off, two L2 loads and (for a CAS lock)
+one atomic, plus the extra time one uncontended TB spends on a larger numLdSt
+than 10; the roofline fraction
+is the floor-weighted ops over the measured time of the dominant kernel's
+cells.  Also the sweep aggregate: each cell counts once at its mean time."""
 import os
 import sys
 
@@ -11,34 +13,68 @@ sys.path.insert(0, ROOT)
 import bench  # noqa: E402
 
 
-class _Probe:
+class _Res:
+    def __init__(self, ops, ms):
+        self.ops, self.elapsed_ms = ops, ms
+
+
+class _HS:
+    """Stand-in for the package: fixed probe figures, and 1-TB runs whose time
+    per op is 2 us at numLdSt 10 and 4 us at 100."""
+
+    class RunConfig:
+        def __init__(self, **kw):
+            self.__dict__.update(kw)
+
     @staticmethod
     def probe_latency(rounds):
         assert rounds > 0
         return {"handoff_ns_median": 700.0, "handoff_ns_min": 400.0, "handoff_ns_max": 800.0,
                 "atomic_rtt_ns": 300.0, "load_rtt_ns": 150.0, "partners": 151, "dev_error_bits": 0}
 
+    @staticmethod
+    def storage_words(cfg):
+        return 16
+
+    @staticmethod
+    def run(cfg, storage):
+        assert cfg.num_tbs == 1
+        us = 2.0 if cfg.num_ldst == 10 else 4.0
+        return _Res(cfg.num_iters, us * cfg.num_iters * 1e-3)
+
+
+def test_floors():
+    floors, lat = bench.lock_floors(_HS, ["spinMutex", "faMutex", "lfTreeBarrUniq"])
+    assert set(floors) == {("spinMutex", 10), ("spinMutex", 100), ("faMutex", 10), ("faMutex", 100)}
+    assert abs(floors[("spinMutex", 10)] - (0.7 + 0.3 + 0.3)) < 1e-9
+    assert abs(floors[("spinMutex", 100)] - (0.7 + 0.3 + 0.3 + 2.0)) < 1e-9
+    assert abs(floors[("faMutex", 10)] - (0.7 + 0.3)) < 1e-9
+    assert abs(floors[("faMutex", 100)] - (0.7 + 0.3 + 2.0)) < 1e-9
+    assert lat["floor_ns"] == {"cas_lock": 1300.0, "queue_lock": 1000.0}
+    assert lat["handoff_ns"] == {"median": 700.0, "min": 400.0, "max": 800.0, "partners": 151}
+
 
 def _rec(prim, tbs, L, us_per_op, ops=1000):
-    return {"prim": prim, "num_tbs": tbs, "num_ldst": L, "ops": ops, "ms": us_per_op * ops * 1e-3}
+    return {"prim": prim, "num_tbs": tbs, "num_ldst": L, "ops": ops, "ms": us_per_op * ops * 1e-3, "wall_s": 0.01}
 
 
-def test_floors_and_fractions():
-    recs = [_rec("spinMutex", 152, 10, 1.6), _rec("spinMutex", 152, 10, 1.4), _rec("faMutex", 152, 10, 1.25),
-            _rec("spinSem1", 152, 10, 2.6), _rec("spinMutex", 304, 10, 9.0), _rec("faMutex", 152, 100, 9.0),
-            _rec("atomicTreeBarrUniq", 152, 10, 0.02)]
-    out = bench.lock_latency(_Probe, recs, 152)
-    assert out["floor_ns"] == {"cas_lock": 1300.0, "queue_lock": 1000.0}
-    cells = out["cells_152x10"]
-    assert set(cells) == {"spinMutex", "faMutex", "spinSem1"}
-    assert cells["spinMutex"]["us_per_op"] == 1.5 and cells["spinMutex"]["floor_us"] == 1.3
-    assert abs(cells["spinMutex"]["frac"] - 1.3 / 1.5) < 1e-3
-    assert cells["faMutex"]["floor_us"] == 1.0 and abs(cells["faMutex"]["frac"] - 0.8) < 1e-3
-    assert abs(cells["spinSem1"]["frac"] - 0.5) < 1e-3
-    assert out["handoff_ns"] == {"median": 700.0, "min": 400.0, "max": 800.0, "partners": 151}
+def test_aggregate_and_roofline():
+    recs = [_rec("spinMutex", 152, 10, 3.0), _rec("spinMutex", 152, 10, 5.0), _rec("faMutex", 152, 10, 2.0),
+            _rec("lfTreeBarrUniq", 152, 10, 0.01)]
+    cells, value, e2e = bench.aggregate(recs)
+    assert set(cells) == {"spinMutex@152/10", "faMutex@152/10", "lfTreeBarrUniq@152/10"}
+    assert abs(cells["spinMutex@152/10"]["us_per_op"] - 4.0) < 1e-9       # mean of its two runs
+    assert abs(value - 3000 / ((4.0 + 2.0 + 0.01) * 1e-3 * 1e3 * 1e-3)) < 1e-6
+    assert abs(e2e - 3000 / 0.03) < 1e-6
+    floors = {("spinMutex", 10): 2.0, ("faMutex", 10): 1.0}
+    roof = bench.latency_roofline(cells, floors, ["spinMutex", "faMutex"], None)
+    assert roof["bound"] == "latency"
+    assert abs(roof["frac"] - (1000 * 2.0 + 1000 * 1.0) / (1000 * 4.0 + 1000 * 2.0)) < 1e-9
+    assert roof["cells"]["spinMutex@152/10"]["frac"] == 0.5
 
 
 def test_every_lock_primitive_has_a_chain():
     locks = [p for p in bench.SWEEP_PRIMS if "Barr" not in p]
     assert sorted(locks) == sorted(bench.LOCK_CHAIN)
     assert {bench.LOCK_CHAIN[p] for p in ("faMutex", "sleepMutex")} == {"queue"}
+    assert bench.HEAD_PRIMS == [p for p in bench.SWEEP_PRIMS if "Sem" not in p]
