@@ -765,6 +765,11 @@ extern "C" int cudaLocksInit(const int maxBlocksPerKernel, const int numMutexes,
   (void)pageAlign;
   if (maxBlocksPerKernel <= 0 || numMutexes <= 0 || numSemaphores <= 0 || NUM_SM <= 0)
     return (int)cudaErrorInitializationError;  // cudaLocks.cu:13-15
+  // The reference's stride (cudaLocks.cu:19) must leave room for a ring of
+  // maxBlocksPerKernel + 1 slots and for the barrier's in/out flags; with few
+  // SMs it can round down to maxBlocksPerKernel or below (even to 0, a
+  // zero-byte barrier buffer).  Such sizes are refused here.
+  if ((maxBlocksPerKernel + NUM_SM) / 16 * 16 <= maxBlocksPerKernel) return (int)cudaErrorInvalidValue;
   if (g_lock) cudaLocksDestroy();
   hs_lock_data* L = nullptr;
   cudaError_t e = cudaMallocHost(&L, sizeof(hs_lock_data));

@@ -417,7 +417,10 @@ typedef struct hs_lock_data {
   unsigned int* semaphoreBuffers;
 } hs_lock_data;
 
-/* cudaLocks.cu:3-81.  Returns a cudaError_t value (0 = cudaSuccess). */
+/* cudaLocks.cu:3-81.  Returns a cudaError_t value (0 = cudaSuccess).  Sizes whose
+ * arrayStride, (maxBlocksPerKernel + NUM_SM) / 16 * 16, would not exceed
+ * maxBlocksPerKernel (a ring of maxBlocksPerKernel + 1 slots would overrun into
+ * the next; a stride of 0 leaves no barrier buffer) return cudaErrorInvalidValue. */
 int cudaLocksInit(const int maxBlocksPerKernel, const int numMutexes, const int numSemaphores, const bool pageAlign,
                   const int NUM_SM);
 /* cudaLocks.cu:83-95 (this one also frees barrierBuffers). */

@@ -13,9 +13,17 @@
 //   per-SM barrier         perSMBarrierBuffers[smID * MAX_BLOCKS * 2 ...]
 //
 // Differences that do not change results:
-//  * waits are bounded; on timeout the wrapper records the failure in
-//    hs_ref_wait_status (per translation unit) and returns as if the wait had
-//    ended, so a caller that must not proceed should check hs_ref_failed();
+//  * waits are bounded and fail fast: a wait that sees no progress for
+//    HS_REF_TIMEOUT_NS records the failure in hs_ref_wait_status (per
+//    translation unit: word 0 the error bits, word 1 the wait site) and ends
+//    the calling CTA -- every thread of the CTA executes PTX `exit` at the same
+//    point, so no critical section runs without its lock and no thread is left
+//    at a CTA barrier.  CTAs waiting on an ended one see the recorded status at
+//    their next poll and end the same way, so the launch completes and the
+//    context stays usable; the host reads the status after the launch
+//    (cudaMemcpyFromSymbol of hs_ref_wait_status in the including file).  The
+//    reference's functions have no error path (they spin forever instead);
+//    TryWait still returns false without ending anything;
 //  * the semaphore keeps its reader/writer admission rules but packs the
 //    writer-waiting flag into bit 31 of word 0 (count), so wait and post are a
 //    CAS and a red instead of a lock round trip (word 1, the reference's CAS
@@ -44,11 +52,16 @@ __device__ __forceinline__ hs::HsEnv hs_ref_env() {
 __device__ __forceinline__ bool hs_ref_failed() {
   return hs::ld_relaxed<hs::GPU>(hs_ref_wait_status) != 0u;
 }
+// End the calling CTA when a block-collective wait failed (ok is the same in
+// every thread of the CTA).
+__device__ __forceinline__ void hs_ref_end_if(bool failed) {
+  if (failed) asm volatile("exit;" ::: "memory");
+}
 
 // --- spin mutex: cudaLocksMutexSpin.cu:13,38,53,81 --------------------------
 __device__ __forceinline__ void cudaMutexSpinLock(const cudaMutex_t mutex, unsigned int* mutexBufferHeads,
                                                   const int NUM_SM) {
-  hs::spin_lock<hs::GPU>(mutexBufferHeads + mutex * NUM_SM, hs_ref_env());
+  hs_ref_end_if(!hs::spin_lock<hs::GPU>(mutexBufferHeads + mutex * NUM_SM, hs_ref_env()));
 }
 __device__ __forceinline__ void cudaMutexSpinUnlock(const cudaMutex_t mutex, unsigned int* mutexBufferHeads,
                                                     const int NUM_SM) {
@@ -57,7 +70,7 @@ __device__ __forceinline__ void cudaMutexSpinUnlock(const cudaMutex_t mutex, uns
 }
 __device__ __forceinline__ void cudaMutexSpinLockLocal(const cudaMutex_t mutex, const unsigned int smID,
                                                        unsigned int* mutexBufferHeads, const int NUM_SM) {
-  hs::spin_lock<hs::GPU>(mutexBufferHeads + mutex * NUM_SM + smID, hs_ref_env());
+  hs_ref_end_if(!hs::spin_lock<hs::GPU>(mutexBufferHeads + mutex * NUM_SM + smID, hs_ref_env()));
 }
 __device__ __forceinline__ void cudaMutexSpinUnlockLocal(const cudaMutex_t mutex, const unsigned int smID,
                                                          unsigned int* mutexBufferHeads, const int NUM_SM) {
@@ -68,7 +81,7 @@ __device__ __forceinline__ void cudaMutexSpinUnlockLocal(const cudaMutex_t mutex
 // --- EBO mutex: cudaLocksMutexEBO.cu:13,59,73,121 ---------------------------
 __device__ __forceinline__ void cudaMutexEBOLock(const cudaMutex_t mutex, unsigned int* mutexBufferHeads,
                                                  const int NUM_SM) {
-  hs::ebo_lock<hs::GPU>(mutexBufferHeads + mutex * NUM_SM, 1u, HS_REF_MAX_BACKOFF, hs_ref_env());
+  hs_ref_end_if(!hs::ebo_lock<hs::GPU>(mutexBufferHeads + mutex * NUM_SM, 1u, HS_REF_MAX_BACKOFF, hs_ref_env()));
 }
 __device__ __forceinline__ void cudaMutexEBOUnlock(const cudaMutex_t mutex, unsigned int* mutexBufferHeads,
                                                    const int NUM_SM) {
@@ -77,7 +90,8 @@ __device__ __forceinline__ void cudaMutexEBOUnlock(const cudaMutex_t mutex, unsi
 }
 __device__ __forceinline__ void cudaMutexEBOLockLocal(const cudaMutex_t mutex, const unsigned int smID,
                                                       unsigned int* mutexBufferHeads, const int NUM_SM) {
-  hs::ebo_lock<hs::GPU>(mutexBufferHeads + mutex * NUM_SM + smID, 1u, HS_REF_MAX_BACKOFF, hs_ref_env());
+  hs_ref_end_if(
+      !hs::ebo_lock<hs::GPU>(mutexBufferHeads + mutex * NUM_SM + smID, 1u, HS_REF_MAX_BACKOFF, hs_ref_env()));
 }
 __device__ __forceinline__ void cudaMutexEBOUnlockLocal(const cudaMutex_t mutex, const unsigned int smID,
                                                         unsigned int* mutexBufferHeads, const int NUM_SM) {
@@ -88,8 +102,8 @@ __device__ __forceinline__ void cudaMutexEBOUnlockLocal(const cudaMutex_t mutex,
 // --- fetch-and-add mutex: cudaLocksMutexFA.cu:13,53,72,115 ------------------
 __device__ __forceinline__ void cudaMutexFALock(const cudaMutex_t mutex, unsigned int* mutexBufferHeads,
                                                 unsigned int* mutexBufferTails, const int NUM_SM) {
-  hs::ticket_lock<hs::GPU>(mutexBufferHeads + mutex * NUM_SM, mutexBufferTails + mutex * NUM_SM, 1000000000u, 0u,
-                           0u, hs_ref_env());
+  hs_ref_end_if(!hs::ticket_lock<hs::GPU>(mutexBufferHeads + mutex * NUM_SM, mutexBufferTails + mutex * NUM_SM,
+                                          1000000000u, 0u, 0u, hs_ref_env()));
 }
 __device__ __forceinline__ void cudaMutexFAUnlock(const cudaMutex_t mutex, unsigned int* mutexBufferTails,
                                                   const int NUM_SM) {
@@ -99,8 +113,8 @@ __device__ __forceinline__ void cudaMutexFAUnlock(const cudaMutex_t mutex, unsig
 __device__ __forceinline__ void cudaMutexFALockLocal(const cudaMutex_t mutex, const unsigned int smID,
                                                      unsigned int* mutexBufferHeads, unsigned int* mutexBufferTails,
                                                      const int NUM_SM) {
-  hs::ticket_lock<hs::GPU>(mutexBufferHeads + mutex * NUM_SM + smID, mutexBufferTails + mutex * NUM_SM + smID,
-                           100000000u, 0u, 0u, hs_ref_env());
+  hs_ref_end_if(!hs::ticket_lock<hs::GPU>(mutexBufferHeads + mutex * NUM_SM + smID,
+                                          mutexBufferTails + mutex * NUM_SM + smID, 100000000u, 0u, 0u, hs_ref_env()));
 }
 __device__ __forceinline__ void cudaMutexFAUnlockLocal(const cudaMutex_t mutex, const unsigned int smID,
                                                        unsigned int* mutexBufferTails, const int NUM_SM) {
@@ -116,7 +130,8 @@ __device__ __forceinline__ unsigned int cudaMutexSleepLock(const cudaMutex_t mut
   unsigned* ring = reinterpret_cast<unsigned*>(mutexBuffers) + (size_t)(mutex * NUM_SM) * arrayStride;
   int r = hs::queue_lock<hs::GPU>(mutexBufferTails + mutex * NUM_SM, ring, 1u, (unsigned)maxRingBufferSize, 0u,
                                   hs_ref_env(), &s_slot);
-  return r < 0 ? 0u : (unsigned)r;
+  hs_ref_end_if(r < 0);
+  return (unsigned)r;
 }
 __device__ __forceinline__ void cudaMutexSleepUnlock(const cudaMutex_t mutex, int* mutexBuffers,
                                                      unsigned int myBufferLoc, const int maxRingBufferSize,
@@ -133,7 +148,8 @@ __device__ __forceinline__ unsigned int cudaMutexSleepLockLocal(const cudaMutex_
   unsigned* ring = reinterpret_cast<unsigned*>(mutexBuffers) + (size_t)(mutex * NUM_SM + smID) * arrayStride;
   int r = hs::queue_lock<hs::GPU>(mutexBufferTails + mutex * NUM_SM + smID, ring, 1u, (unsigned)maxRingBufferSize,
                                   0u, hs_ref_env(), &s_slot);
-  return r < 0 ? 0u : (unsigned)r;
+  hs_ref_end_if(r < 0);
+  return (unsigned)r;
 }
 __device__ __forceinline__ void cudaMutexSleepUnlockLocal(const cudaMutex_t mutex, const unsigned int smID,
                                                           int* mutexBuffers, unsigned int myBufferLoc,
@@ -160,8 +176,8 @@ __device__ __forceinline__ bool cudaSemaphoreSpinTryWait(const cudaSemaphore_t s
 __device__ __forceinline__ void cudaSemaphoreSpinWait(const cudaSemaphore_t sem, const bool isWriter,
                                                       const unsigned int maxSemCount, unsigned int* semaphoreBuffers,
                                                       const int NUM_SM) {
-  hs::sem_wait<hs::GPU>(hs_ref_sem_word(sem, 0, semaphoreBuffers, NUM_SM), isWriter, maxSemCount, false, false, 0u,
-                        0u, hs_ref_env());
+  hs_ref_end_if(!hs::sem_wait<hs::GPU>(hs_ref_sem_word(sem, 0, semaphoreBuffers, NUM_SM), isWriter, maxSemCount,
+                                       false, false, 0u, 0u, hs_ref_env()));
 }
 __device__ __forceinline__ void cudaSemaphoreSpinPost(const cudaSemaphore_t sem, const bool isWriter,
                                                       const unsigned int maxSemCount, unsigned int* semaphoreBuffers,
@@ -180,8 +196,8 @@ __device__ __forceinline__ bool cudaSemaphoreSpinTryWaitLocal(const cudaSemaphor
 __device__ __forceinline__ void cudaSemaphoreSpinWaitLocal(const cudaSemaphore_t sem, const unsigned int smID,
                                                            const bool isWriter, const unsigned int maxSemCount,
                                                            unsigned int* semaphoreBuffers, const int NUM_SM) {
-  hs::sem_wait<hs::GPU>(hs_ref_sem_word(sem, smID, semaphoreBuffers, NUM_SM), isWriter, maxSemCount, false, false,
-                        0u, 0u, hs_ref_env());
+  hs_ref_end_if(!hs::sem_wait<hs::GPU>(hs_ref_sem_word(sem, smID, semaphoreBuffers, NUM_SM), isWriter, maxSemCount,
+                                       false, false, 0u, 0u, hs_ref_env()));
 }
 __device__ __forceinline__ void cudaSemaphoreSpinPostLocal(const cudaSemaphore_t sem, const unsigned int smID,
                                                            const bool isWriter, const unsigned int maxSemCount,
@@ -197,8 +213,8 @@ __device__ __forceinline__ bool cudaSemaphoreEBOTryWait(const cudaSemaphore_t se
 __device__ __forceinline__ void cudaSemaphoreEBOWait(const cudaSemaphore_t sem, const bool isWriter,
                                                      const unsigned int maxSemCount, unsigned int* semaphoreBuffers,
                                                      const int NUM_SM) {
-  hs::sem_wait<hs::GPU>(hs_ref_sem_word(sem, 0, semaphoreBuffers, NUM_SM), isWriter, maxSemCount, true, true, 1u,
-                        HS_REF_MAX_BACKOFF, hs_ref_env());
+  hs_ref_end_if(!hs::sem_wait<hs::GPU>(hs_ref_sem_word(sem, 0, semaphoreBuffers, NUM_SM), isWriter, maxSemCount,
+                                       true, true, 1u, HS_REF_MAX_BACKOFF, hs_ref_env()));
 }
 __device__ __forceinline__ void cudaSemaphoreEBOPost(const cudaSemaphore_t sem, const bool isWriter,
                                                      const unsigned int maxSemCount, unsigned int* semaphoreBuffers,
@@ -213,8 +229,8 @@ __device__ __forceinline__ bool cudaSemaphoreEBOTryWaitLocal(const cudaSemaphore
 __device__ __forceinline__ void cudaSemaphoreEBOWaitLocal(const cudaSemaphore_t sem, const unsigned int smID,
                                                           const bool isWriter, const unsigned int maxSemCount,
                                                           unsigned int* semaphoreBuffers, const int NUM_SM) {
-  hs::sem_wait<hs::GPU>(hs_ref_sem_word(sem, smID, semaphoreBuffers, NUM_SM), isWriter, maxSemCount, true, false, 1u,
-                        HS_REF_MAX_BACKOFF, hs_ref_env());
+  hs_ref_end_if(!hs::sem_wait<hs::GPU>(hs_ref_sem_word(sem, smID, semaphoreBuffers, NUM_SM), isWriter, maxSemCount,
+                                       true, false, 1u, HS_REF_MAX_BACKOFF, hs_ref_env()));
 }
 __device__ __forceinline__ void cudaSemaphoreEBOPostLocal(const cudaSemaphore_t sem, const unsigned int smID,
                                                           const bool isWriter, const unsigned int maxSemCount,
@@ -227,13 +243,13 @@ __device__ __forceinline__ void cudaSemaphoreEBOPostLocal(const cudaSemaphore_t 
 // The per-SM group uses perSM[smID*MAX_BLOCKS + {0,1}] the same way.
 __device__ __forceinline__ void hs_ref_counter_barrier(unsigned* cnt, unsigned n, const bool isMasterThread) {
   __syncthreads();
+  bool ok = true;
   if (isMasterThread) {
     hs::HsEnv env = hs_ref_env();
     const unsigned gen = hs::ld_relaxed<hs::GPU>(cnt + 1);
-    bool ok = true;
     hs::counter_barrier<hs::GPU>(cnt, cnt + 1, n, gen, 0u, env, hs::HS_SITE_BAR_GLOBAL, [] { return true; }, &ok);
   }
-  __syncthreads();
+  hs_ref_end_if(__syncthreads_or(!ok) != 0);
 }
 __device__ __forceinline__ void cudaBarrierAtomic(unsigned int* barrierBuffers, const unsigned int numBarr,
                                                   const bool isMasterThread) {
@@ -270,13 +286,15 @@ __device__ __forceinline__ void hs_ref_flag_barrier(unsigned* inVars, unsigned* 
   }
   __syncthreads();
   const unsigned e = s_gen;
+  bool ok = true;
   if (isMain) {
-    if (hs::scan_flags<hs::GPU>(inVars, numBlocks, e, 0u, env, hs::HS_SITE_BAR_SCAN) && hs::is_master())
-      hs::st_release<hs::GPU>(outVars, e);
+    ok = hs::scan_flags<hs::GPU>(inVars, numBlocks, e, 0u, env, hs::HS_SITE_BAR_SCAN);
+    if (ok && hs::is_master()) hs::st_release<hs::GPU>(outVars, e);
   } else if (hs::is_master()) {
-    hs::wait_until([&] { return (int)(hs::ld_acquire<hs::GPU>(outVars) - e) >= 0; }, [] {}, env, hs::HS_SITE_BAR_GO);
+    ok = hs::wait_until([&] { return (int)(hs::ld_acquire<hs::GPU>(outVars) - e) >= 0; }, [] {}, env,
+                        hs::HS_SITE_BAR_GO);
   }
-  __syncthreads();
+  hs_ref_end_if(__syncthreads_or(!ok) != 0);
 }
 __device__ __forceinline__ void cudaBarrier(unsigned int* barrierBuffers, const int arrayStride,
                                             const unsigned int numBlocksAtBarr) {
@@ -300,15 +318,16 @@ __device__ __forceinline__ void cudaBarrierLocal(unsigned int* barrierBuffers, c
     }
     __syncthreads();
     const unsigned e = s_gen;
+    bool ok = true;
     if (perSM_blockID == 0) {
-      hs::scan_flags<hs::GPU>(inVars, numTBs_perSM, e, 0u, env, hs::HS_SITE_BAR_SCAN);
+      hs_ref_end_if(!hs::scan_flags<hs::GPU>(inVars, numTBs_perSM, e, 0u, env, hs::HS_SITE_BAR_SCAN));
       cudaBarrier(barrierBuffers, arrayStride, numBlocksAtBarr);
       if (hs::is_master()) hs::st_release<hs::GPU>(outVars, e);
     } else if (hs::is_master()) {
-      hs::wait_until([&] { return (int)(hs::ld_acquire<hs::GPU>(outVars) - e) >= 0; }, [] {}, env,
-                     hs::HS_SITE_BAR_GO);
+      ok = hs::wait_until([&] { return (int)(hs::ld_acquire<hs::GPU>(outVars) - e) >= 0; }, [] {}, env,
+                          hs::HS_SITE_BAR_GO);
     }
-    __syncthreads();
+    hs_ref_end_if(__syncthreads_or(!ok) != 0);
   } else {
     hs_ref_flag_barrier(inVars, outVars, numTBs_perSM, perSM_blockID, perSM_blockID == 0);
   }
