@@ -33,6 +33,7 @@ _MODES = {"ref": MODE_REF, "inc": MODE_INC, "slice": MODE_SLICE}
 HS_OK, HS_EINVAL, HS_ETIMEDOUT, HS_ENORES, HS_ECUDA, HS_ENODEV, HS_EMISMATCH = range(7)
 RUN_SYNC_EACH, RUN_KEEP_STATE, RUN_NO_CLUSTER, RUN_REGISTER_CS, RUN_GRAPH, RUN_NO_COHORT = 1, 2, 4, 8, 16, 32
 RUN_CLUSTER_CS = 64
+RUN_NO_GROUP_CTA = 128
 
 # Reference names and ids, main.cu:1224-1256.
 PRIM_NAMES = {
@@ -82,7 +83,7 @@ class _RunResult(ctypes.Structure):
         ("status", ctypes.c_int), ("dev_error_bits", ctypes.c_uint), ("dev_error_site", ctypes.c_uint),
         ("elapsed_ms", ctypes.c_float), ("avg_ms", ctypes.c_float), ("h2d_ms", ctypes.c_float),
         ("d2h_ms", ctypes.c_float), ("ops", ctypes.c_ulonglong), ("launches", ctypes.c_uint),
-        ("cluster", ctypes.c_int), ("cohort", ctypes.c_int),
+        ("cluster", ctypes.c_int), ("cohort", ctypes.c_int), ("tbs_per_cta", ctypes.c_int),
     ]
 
 
@@ -223,6 +224,7 @@ class RunResult:
     launches: int
     cluster: int = 1
     cohort: int = 0
+    tbs_per_cta: int = 1
 
     @property
     def ops_per_s(self) -> float:
@@ -292,7 +294,7 @@ def run(cfg: RunConfig, storage, stream: Optional[int] = None, check: bool = Tru
     s = lib().hs_run(_context(), ctypes.byref(c), ctypes.c_void_p(ptr), on_device,
                      ctypes.c_void_p(stream or 0), ctypes.byref(r))
     res = RunResult(r.status, r.dev_error_bits, r.dev_error_site, r.elapsed_ms, r.avg_ms, r.h2d_ms, r.d2h_ms,
-                    r.ops, r.launches, r.cluster, r.cohort)
+                    r.ops, r.launches, r.cluster, r.cohort, r.tbs_per_cta)
     if check and s:
         raise _err(s)
     return res

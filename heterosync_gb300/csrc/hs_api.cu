@@ -18,6 +18,7 @@ KernelFn syncprim_plan(int prim, int mode, int threads, int num_ldst, size_t* sm
 cudaError_t prepare_smem(KernelFn fn, size_t smem_bytes);
 size_t barrier_tile_bytes(int threads, int num_ldst, int num_tbs, int phys_nsm, size_t base);
 KernelFn prim_cluster_kernel(int mode);
+KernelFn barrier_group_kernel(int prim, int mode);
 cudaError_t launch_ring_init(unsigned* ring, unsigned slots_per_group, unsigned groups, cudaStream_t st);
 cudaError_t launch_fill_lines(unsigned* base, size_t n, size_t stride, unsigned value, cudaStream_t st);
 }  // namespace hs
@@ -572,7 +573,33 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c0, void* storage, int o
     if (cudaOccupancyMaxActiveClusters(&fit, (const void*)fn, &lc) == cudaSuccess && fit >= nsm) cluster = m;
     cudaGetLastError();
   }
-  if (is_barrier(c->prim)) {
+  // Tree barriers whose whole logical-SM groups fit one CTA (m * threads <=
+  // 1024) run each group as one CTA on the register path: the local stage is
+  // the CTA barrier.  Measured (1000 episodes, 256 threads, us per episode):
+  // lfTreeBarrUniqLocalExch at 608 TBs, numLdSt 10: 5.17 against 8.01 flat;
+  // at 304 TBs 3.79 against 5.89 on clusters of 2; at numLdSt 64 it still
+  // beats the bulk-copy tiles (304 TBs: 6.34 against 7.10 for
+  // lfTreeBarrUniq), at numLdSt 100 the tiles win (608 TBs: 12.89 against
+  // 14.22), so up to numLdSt 64.  Every group CTA must be resident at once.
+  int block = c->threads, tbs_per_cta = 1;
+  if (is_barrier(c->prim) && c->mode != HS_MODE_SLICE && c->num_ldst <= 64 &&
+      !(c->flags & (HS_RUN_NO_CLUSTER | HS_RUN_NO_GROUP_CTA)) && c->skip_tb < 0 && variant != PV_NAIVE &&
+      variant != PV_NAIVE_ALL) {
+    const int nb = c->num_tbs < nsm ? c->num_tbs : nsm;
+    const int m = c->num_tbs / nb;
+    KernelFn gfn = barrier_group_kernel(c->prim, c->mode);
+    int per_sm = 0;
+    if (gfn && m >= 2 && c->num_tbs % nb == 0 && m * c->threads <= 1024 && m * c->threads <= ctx->max_tpb &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gfn, m * c->threads, 0) == cudaSuccess &&
+        (long long)per_sm * ctx->nsm >= nb) {
+      fn = gfn;
+      smem = 0;
+      block = m * c->threads;
+      tbs_per_cta = m;
+    }
+    cudaGetLastError();
+  }
+  if (is_barrier(c->prim) && tbs_per_cta == 1) {
     const int nb = c->num_tbs < nsm ? c->num_tbs : nsm;
     const int m = c->num_tbs / nb;
     if (!(c->flags & HS_RUN_NO_CLUSTER) && c->skip_tb < 0 && c->num_tbs % nb == 0 && (m == 2 || m == 4 || m == 8) &&
@@ -610,7 +637,7 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c0, void* storage, int o
   // only where a semaphore writer moves 4 or more chunks (spinSem1 at 608 TBs
   // 4.72 against 5.40); slower for mutexes (faMutex 4.34 against 3.26) and
   // smaller writers, so by default only there.
-  int grid = c->num_tbs;
+  int grid = tbs_per_cta > 1 ? c->num_tbs / tbs_per_cta : c->num_tbs;
   const bool sem_prim = c->prim >= 8 && c->prim <= 15;
   const int sem_numSM = c->num_tbs < nsm ? c->num_tbs : nsm;
   const int sem_k = sem_prim ? (c->num_tbs + sem_numSM - 1) / sem_numSM : 1;  // chunks a semaphore writer owns
@@ -661,7 +688,9 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c0, void* storage, int o
 
   d.cluster = cluster;
   d.variant = variant;
+  d.grp = tbs_per_cta;
   r->cluster = cluster;
+  r->tbs_per_cta = tbs_per_cta;
   // global spin / FA mutex, or global semaphore (its writers), with more than
   // one TB: the die-aware cohort form
   if ((c->prim == 4 || c->prim == 7 || (c->prim >= 8 && c->prim <= 15)) && c->num_tbs > 1 && grid == c->num_tbs &&
@@ -681,7 +710,7 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c0, void* storage, int o
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   lc.gridDim = dim3((unsigned)grid);
-  lc.blockDim = dim3((unsigned)c->threads);
+  lc.blockDim = dim3((unsigned)block);
   lc.dynamicSmemBytes = smem;
   lc.stream = st;
   lc.attrs = attr;

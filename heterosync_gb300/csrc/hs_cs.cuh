@@ -18,8 +18,11 @@ __device__ __forceinline__ size_t chunk_words(int T, int L) { return (size_t)T *
 // into registers, one CTA barrier, then stores.  Stores of a pass never touch
 // lines a later pass loads, and a later pass only overwrites lines an earlier
 // pass already loaded, so one barrier per pass suffices.
+// `tid` is the thread's index within the T threads that work on the chunk
+// (threadIdx.x, or its index within a sub-block when one CTA hosts several
+// logical TBs; every sub-block then passes through the same CTA barriers).
 template <int MAXV>
-__device__ __forceinline__ void cs_ref_shift(unsigned* chunk, int T, int L) {
+__device__ __forceinline__ void cs_ref_shift(unsigned* chunk, int T, int L, int tid = threadIdx.x) {
   const int R = T >> 4;
   const int rw4 = (L + 1) * 4;
   uint4* c4 = reinterpret_cast<uint4*>(chunk);
@@ -32,7 +35,7 @@ __device__ __forceinline__ void cs_ref_shift(unsigned* chunk, int T, int L) {
     int idx[MAXV];
 #pragma unroll
     for (int u = 0; u < MAXV; ++u) {
-      const int t = threadIdx.x + u * T;
+      const int t = tid + u * T;
       idx[u] = -1;
       if (t < nitems) {
         const int h = t / per_region;
@@ -49,7 +52,7 @@ __device__ __forceinline__ void cs_ref_shift(unsigned* chunk, int T, int L) {
 
 // INC: every word of lines 1..L of every region gets +1.
 template <int MAXV>
-__device__ __forceinline__ void cs_inc(unsigned* chunk, int T, int L) {
+__device__ __forceinline__ void cs_inc(unsigned* chunk, int T, int L, int tid = threadIdx.x) {
   const int R = T >> 4;
   const int rw4 = (L + 1) * 4;
   const int per_region = L * 4;
@@ -60,7 +63,7 @@ __device__ __forceinline__ void cs_inc(unsigned* chunk, int T, int L) {
     int idx[MAXV];
 #pragma unroll
     for (int u = 0; u < MAXV; ++u) {
-      const int t = base + threadIdx.x + u * T;
+      const int t = base + tid + u * T;
       idx[u] = -1;
       if (t < nitems) {
         const int h = t / per_region;
@@ -418,10 +421,10 @@ __device__ __forceinline__ bool cs_read_tma(const RunDesc& d, int chunk, TmaCtx&
 template <int V> struct Bounds { static constexpr int kThreads = V <= 4 ? 1024 : (V <= 8 ? 512 : 256); };
 
 template <int MODE, int V>
-__device__ __forceinline__ void cs_chunk(const RunDesc& d, int chunk) {
+__device__ __forceinline__ void cs_chunk(const RunDesc& d, int chunk, int tid = threadIdx.x) {
   unsigned* c = d.data + (size_t)chunk * chunk_words(d.T, d.L);
-  if constexpr (MODE == M_REF) cs_ref_shift<V>(c, d.T, d.L);
-  else cs_inc<V>(c, d.T, d.L);
+  if constexpr (MODE == M_REF) cs_ref_shift<V>(c, d.T, d.L, tid);
+  else cs_inc<V>(c, d.T, d.L, tid);
 }
 
 __device__ __forceinline__ unsigned* group_line(const RunDesc& d, int g, int k) {

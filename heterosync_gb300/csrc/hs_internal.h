@@ -43,6 +43,7 @@ struct RunDesc {
   unsigned long long timeout_ns;
   int skip_tb;          // logical TB that never arrives at a barrier (-1: none)
   int cluster;          // CTAs per cluster for barrier kernels (1: no clusters)
+  int grp;              // tree barriers: logical TBs one CTA hosts (0 or 1: one CTA per TB)
   // line offsets inside `locks`
   int l_glob;           // global barrier: +0 count, +1 gen, +2 go
   int l_gflag;          // global barrier flags (dense, one word per group)

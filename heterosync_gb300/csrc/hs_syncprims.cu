@@ -460,6 +460,50 @@ __global__ void __launch_bounds__(TMA ? 256 : Bounds<V>::kThreads, TMA ? 4 : 102
   }
 }
 
+// Tree barrier with each logical-SM group in ONE CTA: d.grp = m logical TBs of
+// T threads share a CTA of m * T threads, physical CTA g hosting group g
+// (logical TB g + r * nb runs on threads [r * T, (r + 1) * T)).  The local
+// stage is then the CTA barrier itself (bar.sync: no L2 round trip and no
+// release fence, where a GPU-scope fence costs 135-320 ns and a flag hand-off
+// 460 ns relaxed, 810 ns with st.release on this part); a group's members run
+// their critical sections side by side, every sub-block passing through the
+// same CTA barriers inside them; the local exchange only touches chunks of the
+// same group (TB b's partner b + nb is its next member), so CTA-scope ordering
+// covers it.  The global stage is the one the one-TB-per-SM tree runs among the
+// nb group leaders (a counter barrier, or flags scanned by group 0 and one
+// release word).  Register path only; m * T <= 1024, every group whole.
+template <bool LF, bool EXCH, int MODE, int V>
+__global__ void __launch_bounds__(1024, 1) k_barrier_grp(RunDesc d) {
+  const int T = d.T;
+  const int nb = (int)gridDim.x;
+  const int Gd = d.num_tbs;
+  const int g = (int)blockIdx.x;
+  const int r = (int)threadIdx.x / T;
+  const int tid = (int)threadIdx.x - r * T;
+  const HsEnv env{d.status, d.timeout_ns};
+  __shared__ BarState s_init;
+  if (is_master()) {
+    s_init.lgen = 0u;
+    s_init.ggen = LF ? ld_relaxed<GPU>(d.locks + (size_t)(d.l_glob + 2) * kLineWords)
+                     : ld_relaxed<GPU>(d.locks + (size_t)(d.l_glob + 1) * kLineWords);
+  }
+  __syncthreads();
+  BarState s = s_init;
+  const int phases = EXCH ? 2 : 1;
+  int cur = g + r * nb;
+  for (int i = 0; i < d.iters; ++i) {
+    for (int ph = 0; ph < phases; ++ph) {
+      if (ph == 1) {
+        __syncthreads();  // the local barrier: every member's critical section is done
+        cur = (cur + nb) % Gd;
+      }
+      cs_chunk<MODE, V>(d, cur, tid);
+    }
+    if (!tree_barrier<LF>(d, g, 0, 1, nb, s, env)) return;
+    cur = (cur + 1) % Gd;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Ring initialisation: slot 0 of every group's ring = 1, the rest = -1
 // (cudaLocks.cu:58-65).
@@ -474,6 +518,29 @@ __global__ void k_ring_init(unsigned* ring, unsigned slots_per_group, unsigned g
 // Host-side dispatch.
 // ---------------------------------------------------------------------------
 using KernelFn = void (*)(RunDesc);
+
+// The group-CTA tree barrier kernel of a barrier primitive (REF and INC modes).
+KernelFn barrier_group_kernel(int prim, int mode) {
+  if (mode == M_REF) {
+    switch (prim) {
+      case P_ATOMIC_TREE: return k_barrier_grp<false, false, M_REF, 8>;
+      case P_ATOMIC_TREE_EXCH: return k_barrier_grp<false, true, M_REF, 8>;
+      case P_LF_TREE: return k_barrier_grp<true, false, M_REF, 8>;
+      case P_LF_TREE_EXCH: return k_barrier_grp<true, true, M_REF, 8>;
+      default: return nullptr;
+    }
+  }
+  if (mode == M_INC) {
+    switch (prim) {
+      case P_ATOMIC_TREE: return k_barrier_grp<false, false, M_INC, 8>;
+      case P_ATOMIC_TREE_EXCH: return k_barrier_grp<false, true, M_INC, 8>;
+      case P_LF_TREE: return k_barrier_grp<true, false, M_INC, 8>;
+      case P_LF_TREE_EXCH: return k_barrier_grp<true, true, M_INC, 8>;
+      default: return nullptr;
+    }
+  }
+  return nullptr;
+}
 
 template <int MODE, int V, bool TMA>
 static KernelFn pick(int prim) {

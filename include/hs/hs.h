@@ -53,9 +53,12 @@ enum {
   HS_RUN_NO_COHORT = 32,  /* global spin / FA mutexes and global semaphores' writers: one lock word for the
                              whole GPU instead of the die-aware cohort (a lock per die, homed on it, handed
                              on within the die) */
-  HS_RUN_CLUSTER_CS = 64  /* global mutexes and semaphores with numLdSt > 32: one thread-block cluster per
+  HS_RUN_CLUSTER_CS = 64, /* global mutexes and semaphores with numLdSt > 32: one thread-block cluster per
                              logical TB, the critical section split over its SMs, for every such run (by
                              default only semaphores whose writers own 4 or more chunks, where it is faster) */
+  HS_RUN_NO_GROUP_CTA = 128 /* tree barriers: one CTA per logical TB even where a whole logical-SM group
+                               fits one CTA (by default such a group, numLdSt <= 64, runs as one CTA of
+                               numTBs_perSM x threads, its local stage the CTA barrier) */
 };
 
 /* One run of one SyncPrims primitive: `repeats` launches of `num_tbs` TBs of
@@ -88,6 +91,7 @@ typedef struct hs_run_result {
   unsigned launches;            /* kernels launched by this call */
   int cluster;                  /* tree barriers: CTAs per thread-block cluster (1: no clusters) */
   int cohort;                   /* global mutexes and semaphores: 1 if the die-aware cohort form ran */
+  int tbs_per_cta;              /* tree barriers: logical TBs per CTA (1: one CTA per TB) */
 } hs_run_result;
 
 typedef struct hs_ctx hs_ctx;

@@ -106,3 +106,26 @@ def test_hip_extension_storage_and_closed_form(hs):
         assert hs.storage_words(a) == hs.storage_words(b)
         init = np.arange(hs.storage_words(a), dtype=np.uint32)
         assert np.array_equal(hs.expected_storage(a, init), hs.expected_storage(b, init))
+
+
+def test_run_structs_match_the_header(hs, tmp_path):
+    """The ctypes mirrors of hs_run_config and hs_run_result have the C layout
+    (size and the offset of the last field), compiled from include/hs/hs.h."""
+    import os
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc")
+    if not cc:
+        import pytest
+        pytest.skip("gcc not found")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "hs/hs.h"\n'
+                   'int main(void){printf("%zu %zu %zu %zu\\n", sizeof(hs_run_config), '
+                   'offsetof(hs_run_config, flags), sizeof(hs_run_result), offsetof(hs_run_result, tbs_per_cta));'
+                   'return 0;}\n')
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I" + os.path.join(root, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert got == [ctypes.sizeof(hs._RunConfig), hs._RunConfig.flags.offset, ctypes.sizeof(hs._RunResult),
+                   hs._RunResult.tbs_per_cta.offset]

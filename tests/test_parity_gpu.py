@@ -118,30 +118,56 @@ def test_uneven_barrier_groups_complete(hs, oracle):
 
 @pytest.mark.parametrize("prim", [0, 1, 2, 3])
 @pytest.mark.parametrize("mult", [2, 4])
-@pytest.mark.parametrize("L", [10, 64])
+@pytest.mark.parametrize("L", [10, 64, 100])
 def test_barrier_groups_on_clusters(hs, oracle, prim, mult, L):
-    """numTBs = mult * NUM_SM: each logical-SM group runs as one thread-block
-    cluster (local stage = hardware cluster barrier); the result equals the
-    flat launch's and the golden's, on the register path (numLdSt 10) and the
-    tiled bulk-copy path (numLdSt 64)."""
+    """numTBs = mult * NUM_SM: each logical-SM group runs as one CTA of mult x
+    256 threads (numLdSt <= 64, register path: the local stage is the CTA
+    barrier), or as one thread-block cluster (local stage = hardware cluster
+    barrier), or flat; every form's result equals the golden's, on the register
+    path and the tiled bulk-copy path (numLdSt 64 and 100 without group CTAs)."""
     nsm = hs.device_info()["nsm"]
     G = mult * nsm
     outs = []
-    for flags in (0, hs.RUN_NO_CLUSTER):
+    for flags in (0, hs.RUN_NO_GROUP_CTA, hs.RUN_NO_CLUSTER):
         cfg = hs.RunConfig(prim=prim, num_ldst=L, num_tbs=G, num_iters=4, threads=256, repeats=2, mode="inc",
                            flags=flags, timeout_ns=5_000_000_000)
         init = _init(hs.storage_words(cfg), prim + 7 * mult)
         st = init.copy()
         res = hs.run(cfg, st)
-        # clusters of `mult` are used when numTBs / mult of them can be resident
-        # (at 4 per SM the GPCs do not hold every cluster of 4: flat launch)
-        assert res.status == 0 and res.cluster in ((mult, 1) if flags == 0 else (1,))
-        if mult == 2 and flags == 0:
-            assert res.cluster == 2
+        assert res.status == 0
+        if flags == 0 and L <= 64:
+            assert res.tbs_per_cta == mult and res.cluster == 1   # one CTA per logical-SM group
+        else:
+            assert res.tbs_per_cta == 1
+            # clusters of `mult` are used when numTBs / mult of them can be resident
+            # (at 4 per SM the GPCs do not hold every cluster of 4: flat launch)
+            assert res.cluster in ((mult, 1) if flags != hs.RUN_NO_CLUSTER else (1,))
+            if mult == 2 and flags != hs.RUN_NO_CLUSTER:
+                assert res.cluster == 2
         assert np.array_equal(st, hs.expected_storage(cfg, init))
         outs.append(st)
     want = oracle.golden(prim, 256, L, G, 4, 2, nsm, True, init)
-    assert np.array_equal(outs[0], want) and np.array_equal(outs[1], want)
+    for o in outs:
+        assert np.array_equal(o, want)
+
+
+@pytest.mark.parametrize("prim", [0, 1, 2, 3])
+@pytest.mark.parametrize("T,mult,nsm", [(128, 8, 0), (64, 4, 6), (32, 16, 5), (256, 2, 3), (16, 3, 4)])
+@pytest.mark.parametrize("mode", ["ref", "inc"])
+def test_barrier_group_cta_shapes(hs, oracle, prim, T, mult, nsm, mode):
+    """The group-CTA form at other shapes: up to 16 logical TBs per CTA,
+    half-warp TBs, logical NUM_SM below the device's, reference and INC data
+    modes; three launches (the generations carry across launches); equal to the
+    literal golden."""
+    dev_nsm = hs.device_info()["nsm"]
+    n = nsm or dev_nsm
+    cfg = hs.RunConfig(prim=prim, num_ldst=9, num_tbs=mult * n, num_iters=5, threads=T, repeats=3, mode=mode,
+                       nsm=nsm, timeout_ns=5_000_000_000)
+    init = _init(hs.storage_words(cfg), 31 * prim + mult)
+    st = init.copy()
+    res = hs.run(cfg, st)
+    assert res.status == 0 and res.tbs_per_cta == mult
+    assert np.array_equal(st, oracle.golden(prim, T, 9, mult * n, 5, 3, n, mode == "inc", init))
 
 
 @pytest.mark.parametrize("prim", [20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30, 31])
