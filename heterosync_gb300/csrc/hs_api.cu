@@ -349,7 +349,7 @@ struct hs_ctx {
   size_t sink_cap = 0;
   void* staging = nullptr;
   size_t staging_cap = 0;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // launch, H2D, D2H pairs
   // HS_RUN_GRAPH: the last captured repeats and what they were captured for
   cudaStream_t gstream = nullptr;  // capture stream when the caller passes the legacy default stream
   cudaGraphExec_t gexec = nullptr;
@@ -770,12 +770,17 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c0, void* storage, int o
   }
   hs_note_launches(r->launches);
   if (!on_device) {
+    HS_CK(cudaEventRecord(ctx->ev[4], st));
     HS_CK(cudaMemcpyAsync(storage, dev, bytes, cudaMemcpyDeviceToHost, st));
+    HS_CK(cudaEventRecord(ctx->ev[5], st));
   }
   if (lst != st) HS_CK(cudaStreamSynchronize(lst));
   HS_CK(cudaStreamSynchronize(st));
   HS_CK(cudaEventElapsedTime(&r->elapsed_ms, ctx->ev[0], ctx->ev[1]));
-  if (!on_device) HS_CK(cudaEventElapsedTime(&r->h2d_ms, ctx->ev[2], ctx->ev[3]));
+  if (!on_device) {
+    HS_CK(cudaEventElapsedTime(&r->h2d_ms, ctx->ev[2], ctx->ev[3]));
+    HS_CK(cudaEventElapsedTime(&r->d2h_ms, ctx->ev[4], ctx->ev[5]));
+  }
   r->avg_ms = c->repeats ? r->elapsed_ms / c->repeats : 0.f;
   r->ops = (unsigned long long)c->num_tbs * c->num_iters * c->repeats;
   s = read_status(ctx, st, r);
@@ -786,8 +791,10 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c0, void* storage, int o
 // The reference's host API: cudaLocks.cu:3-95 and the Create functions.
 // ---------------------------------------------------------------------------
 static hs_lock_data* g_lock = nullptr;
+static float g_lock_copy_ms = 0.f;
 
 extern "C" hs_lock_data* hs_lock_data_get(void) { return g_lock; }
+extern "C" float hs_locks_init_copy_ms(void) { return g_lock_copy_ms; }
 
 extern "C" int cudaLocksInit(const int maxBlocksPerKernel, const int numMutexes, const int numSemaphores,
                              const bool pageAlign, const int NUM_SM) {
@@ -821,7 +828,16 @@ extern "C" int cudaLocksInit(const int maxBlocksPerKernel, const int numMutexes,
   // rings: first slot of every ring 1, the rest -1 (cudaLocks.cu:58-65)
   std::vector<int> ring(stride * numMutexes, -1);
   for (size_t i = 0; i < ring.size(); i += stride) ring[i] = 1;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;  // the copy is timed, as cudaLocks.cu:66-74 times it
+  if ((e = cudaEventCreate(&e0)) != cudaSuccess) return (int)e;
+  if ((e = cudaEventCreate(&e1)) != cudaSuccess) { cudaEventDestroy(e0); return (int)e; }
+  cudaEventRecord(e0, 0);
   e = cudaMemcpy(L->mutexBuffers, ring.data(), ring.size() * 4, cudaMemcpyHostToDevice);
+  cudaEventRecord(e1, 0);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&g_lock_copy_ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
   if (e != cudaSuccess) return (int)e;
   e = cudaDeviceSynchronize();
   if (e != cudaSuccess) return (int)e;

@@ -134,17 +134,18 @@ template <int S, bool EBO, bool UNIQ, int MODE, int V, bool TMA>
 __device__ __forceinline__ void sem_loop(const RunDesc& d, int b, int numSM, int k, bool writer, unsigned* st,
                                          int rchunk, TmaCtx& tma, const HsEnv& env) {
   const int Gd = d.num_tbs;
-  unsigned* local = nullptr;  // the writer's die cohort word (cohort runs only)
+  unsigned* const* local = nullptr;  // the writer's die cohort lines (cohort runs only)
   if constexpr (S == GPU && !UNIQ) {
     if (d.cohort && writer) {
       unsigned sm;
       asm volatile("mov.u32 %0, %%smid;" : "=r"(sm));
-      local = d.coh[3 * (d.die_map[sm & 255u] & 1)];
+      local = d.coh + 3 * (d.die_map[sm & 255u] & 1);
     }
   }
   for (int i = 0; i < d.iters; ++i) {
-    unsigned pc = 0, others = 0;  // cohort state (master thread)
-    const bool got = local ? cohort_sem_writer_wait(local, st, d.sem_max, EBO, d.bo_min, d.bo_max, env, pc, others)
+    unsigned my = 0, pc = 0, snap = 0;  // cohort state (master thread)
+    const bool got = local ? cohort_sem_writer_wait(local[0], local[1], st, d.sem_max, EBO, d.bo_min, d.bo_max, env,
+                                                    my, pc, snap)
                            : sem_wait<S>(st, writer, d.sem_max, EBO, !UNIQ, d.bo_min, d.bo_max, env);
     if (!got) break;
     bool ok = true;
@@ -159,7 +160,7 @@ __device__ __forceinline__ void sem_loop(const RunDesc& d, int b, int numSM, int
       if constexpr (TMA) ok = cs_read_tma(d, rchunk, tma, env, d.sink + b);
       else cs_read(d.data + (size_t)rchunk * chunk_words(d.T, d.L), d.T, d.L, d.sink + b);
     }
-    if (local) cohort_sem_writer_post(local, st, d.sem_max, pc, others);
+    if (local) cohort_sem_writer_post(local[1], st, d.sem_max, my, pc, snap);
     else sem_post<S>(st, writer, d.sem_max);
     if (!ok) break;
   }

@@ -431,6 +431,10 @@ int cudaLocksInit(const int maxBlocksPerKernel, const int numMutexes, const int 
 int cudaLocksDestroy(void);
 /* The lock data cudaLocksInit filled in (the reference's cpuLockData, pinned host memory). */
 hs_lock_data* hs_lock_data_get(void);
+/* Device time (CUDA events) of the last cudaLocksInit's host-to-device copy of
+ * the ring-buffer slots: the figure the reference prints as "memcpy H->D 1"
+ * (cudaLocks.cu:66-74). */
+float hs_locks_init_copy_ms(void);
 /* cudaLocksMutexSpin.cu:4, cudaLocksMutexEBO.cu:6, cudaLocksMutexFA.cu:6, cudaLocksMutexSleep.cu:6 */
 int cudaMutexCreateSpin(unsigned int* const handle, const int mutexNumber);
 int cudaMutexCreateEBO(unsigned int* const handle, const int mutexNumber);

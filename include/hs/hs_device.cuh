@@ -434,21 +434,20 @@ __device__ __forceinline__ bool sem_wait(unsigned* st, bool writer, unsigned max
 }
 // Die-aware (cohort) writers of a global semaphore.  Writers exclude one
 // another and every reader, so, like the cohort mutexes, the writers of one die
-// form a cohort with a local word homed on that die (the cohort_tas_lock
-// encoding: [31:16] waiters, [15:1] passes so far, [0] held).  A writer that
-// takes the local word without inheriting (passes == 0) takes the semaphore by
-// the reference's writer rule (count == maxc, else set writer-waiting); on
-// release, a writer with a waiter on its die passes the semaphore to it (at
+// form a cohort queued on a ticket lock homed on that die (the
+// cohort_ticket_lock encoding: local turn = (ticket << 6) | passes).  A writer
+// whose turn comes without a pass takes the semaphore by the reference's writer
+// rule (count == maxc, else set writer-waiting); on release, a writer with
+// writers queued behind it on its die hands the semaphore to the next one (at
 // most kCohortMaxPass times in a row) instead of posting, otherwise it posts
-// (count += maxc) and frees the local word.  A pass is what the reference's
+// (count += maxc) and advances the turn.  A hand-over is what the reference's
 // rules would give as well: a waiting writer has writer-waiting set, so no
 // reader can enter between the post and that writer's acquisition; here the
-// count simply stays 0 across it.  The hand-off between two writers of a die
-// then touches only a line homed on that die, and only one writer per die
-// polls the semaphore word.
-__device__ __forceinline__ bool cohort_sem_writer_wait(unsigned* local, unsigned* st, unsigned maxc, bool ebo,
-                                                       unsigned bmin, unsigned bmax, const HsEnv& env, unsigned& pc,
-                                                       unsigned& others) {
+// count simply stays 0 across it.  A hand-over touches only the die's own
+// lines (no CAS at all), and only one writer per die polls the semaphore word.
+__device__ __forceinline__ bool cohort_sem_writer_wait(unsigned* lt, unsigned* lu, unsigned* st, unsigned maxc,
+                                                       bool ebo, unsigned bmin, unsigned bmax, const HsEnv& env,
+                                                       unsigned& my, unsigned& pc, unsigned& snap) {
   int ok = 0;
   if (is_master()) {
     unsigned b = bmin;
@@ -458,21 +457,15 @@ __device__ __forceinline__ bool cohort_sem_writer_wait(unsigned* local, unsigned
         b = ebo_next(b, bmax);
       }
     };
-    atomicAdd(local, 1u << 16);  // register as a waiter
-    unsigned got = 0;
-    ok = wait_until_p(
-        [&] {
-          const unsigned v = ld_relaxed<GPU>(local);
-          if (v & 1u) return false;
-          if (atom_cas_acquire<GPU>(local, v, (v | 1u) - (1u << 16)) != v) return false;
-          got = v;
-          return true;
-        },
-        [&] { return ld_relaxed<GPU>(local); }, backoff, env, HS_SITE_SEM_WAIT);
-    pc = (got >> 1) & 0x7FFFu;
-    others = (got >> 16) - 1u;
-    if (ok && pc == 0u) {  // the cohort does not hold the semaphore: take it by the writer rule
-      b = bmin;
+    my = atom_inc_relaxed<GPU>(lt, kCohortTicketWrap);
+    unsigned cur = 0;
+    // the die's ticket queue is this build's own and has no backoff; the EBO
+    // backoff applies where the reference's writers back off, on the semaphore
+    ok = wait_until_p([&] { cur = ld_acquire<GPU>(lu); return (cur >> 6) == my; }, [&] { return cur; }, [] {}, env,
+                      HS_SITE_SEM_WAIT);
+    pc = cur & 63u;
+    snap = ld_relaxed<GPU>(lt);  // tickets taken so far; needed only at release
+    if (ok && pc == 0u) {  // the die's cohort does not hold the semaphore: take it by the writer rule
       ok = wait_until_p(
           [&] {
             const unsigned s = ld_relaxed<GPU>(st);
@@ -485,15 +478,16 @@ __device__ __forceinline__ bool cohort_sem_writer_wait(unsigned* local, unsigned
   }
   return __syncthreads_or(ok) != 0;
 }
-__device__ __forceinline__ void cohort_sem_writer_post(unsigned* local, unsigned* st, unsigned maxc, unsigned pc,
-                                                       unsigned others) {
+__device__ __forceinline__ void cohort_sem_writer_post(unsigned* lu, unsigned* st, unsigned maxc, unsigned my,
+                                                       unsigned pc, unsigned snap) {
   __syncthreads();  // every thread's critical-section stores precede the release
   if (is_master()) {
-    if (others != 0u && pc + 1u < kCohortMaxPass) {
-      red_release_add<GPU>(local, 1u);  // pass the semaphore to a writer of this die
+    const unsigned next = (my >= kCohortTicketWrap) ? 0u : my + 1u;
+    if (snap != next && pc + 1u < kCohortMaxPass) {
+      st_release<GPU>(lu, (next << 6) | (pc + 1u));  // hand the semaphore to the next writer of this die
     } else {
       red_release_add<GPU>(st, maxc);
-      red_release_add<GPU>(local, 0u - (2u * pc + 1u));
+      st_release<GPU>(lu, next << 6);
     }
   }
 }

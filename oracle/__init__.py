@@ -123,6 +123,32 @@ def ref_run(prim: int, T: int, L: int, num_tbs: int, iters: int, repeats: int, i
     return s, float(ms.value)
 
 
+def ref_refcounter_module() -> str:
+    return os.path.join(REF_DIR, "refcounter_sm100.cubin")
+
+
+def ref_refcounter(num_sharers: int, num_tbs: int, tb_size: int, num_repeats: int):
+    """The reference's own refCounter kernel (one launch, refCounter.cu:24-82);
+    returns (counters0, counters1, del0, del1, ms)."""
+    if not os.path.exists(ref_refcounter_module()):
+        raise FileNotFoundError("no reference refCounter module")
+    L = _reflib()
+    if not hasattr(L, "_rc_ready"):
+        L.hs_ref_refcounter.argtypes = [ctypes.c_char_p] + [ctypes.c_int] * 4 + [ctypes.c_void_p] * 4 + \
+            [ctypes.POINTER(ctypes.c_float)]
+        L._rc_ready = True
+    thrs = num_tbs * tb_size
+    nc = thrs // num_sharers
+    c0, c1 = np.zeros(nc, np.uint32), np.zeros(nc, np.uint32)
+    d0, d1 = np.zeros(thrs, np.uint32), np.zeros(thrs, np.uint32)
+    ms = ctypes.c_float()
+    rc = L.hs_ref_refcounter(ref_refcounter_module().encode(), num_sharers, num_tbs, tb_size, num_repeats,
+                             c0.ctypes.data, c1.ctypes.data, d0.ctypes.data, d1.ctypes.data, ctypes.byref(ms))
+    if rc:
+        raise RuntimeError("reference refCounter run refused/failed (%d): %s" % (rc, L.hs_ref_last_error().decode()))
+    return c0, c1, d0, d1, float(ms.value)
+
+
 def twin_run(prim: int, T: int, L: int, num_tbs: int, iters: int, repeats: int, nsm: int, mode: int,
              init: np.ndarray, threads: int = 0):
     """Host std::thread run of the same algorithm; returns (final storage, seconds)."""

@@ -285,3 +285,71 @@ extern "C" int hs_ref_run(const char* cubin, int T, int prim, int L, int numTBs,
   cuMemFreeHost(ld);
   return 0;
 }
+
+// The reference's refCounter kernel (cuda/relaxedAtomics/uvm/refCounter/
+// refCounter_kernel.cu:4-55) with its host's sizes and one launch
+// (refCounter.cu:24-82, numRuns = 1): numCounters = numThrs / numSharers,
+// numSharingGroups = numTBs / numSharers, numCounters_perSharingGroup =
+// numCounters / numSharingGroups.  The kernel has no waits (uniform loops of
+// atomics and CTA barriers), so it cannot hang.  Returns the final counters0/1
+// (numCounters words each) and del0/1 (numThrs words each).  Sizes whose
+// counter index (sharing group * per-group + threadIdx.x) would leave the
+// arrays are refused (1).
+extern "C" int hs_ref_refcounter(const char* cubin, int numSharers, int numTBs, int tbSize, int numRepeats,
+                                 uint32_t* counters0, uint32_t* counters1, uint32_t* del0, uint32_t* del1,
+                                 float* elapsed_ms) {
+  int r = ensure_ctx();
+  if (r) return r;
+  CK(cuCtxSetCurrent(g_ctx));
+  if (numSharers <= 0 || numTBs <= 0 || tbSize <= 0 || tbSize > 256 || numSharers > numTBs || numRepeats < 0 ||
+      numTBs % numSharers != 0) {
+    g_msg = "bad arguments";
+    return 1;
+  }
+  const unsigned numThrs = (unsigned)tbSize * (unsigned)numTBs;
+  const unsigned numCounters = numThrs / (unsigned)numSharers;
+  const unsigned numGroups = (unsigned)numTBs / (unsigned)numSharers;
+  const unsigned perGroup = numCounters / numGroups;
+  if ((numGroups - 1u) * perGroup + (unsigned)tbSize > numCounters) { g_msg = "counter index out of range"; return 1; }
+  CUmodule mod;
+  auto it = g_mods.find(cubin);
+  if (it == g_mods.end()) {
+    CK(cuModuleLoad(&mod, cubin));
+    g_mods[cubin] = mod;
+  } else {
+    mod = it->second;
+  }
+  CUfunction fn;
+  if ((r = find_kernel(mod, "refCounter_kernel", &fn))) return r;
+  CUdeviceptr c0, c1, d0, d1;
+  CK(cuMemAlloc(&c0, (size_t)numCounters * 4));
+  CK(cuMemAlloc(&c1, (size_t)numCounters * 4));
+  CK(cuMemAlloc(&d0, (size_t)numThrs * 4));
+  CK(cuMemAlloc(&d1, (size_t)numThrs * 4));
+  CK(cuMemsetD32(c0, 0, numCounters));
+  CK(cuMemsetD32(c1, 0, numCounters));
+  CK(cuMemsetD32(d0, 0, numThrs));
+  CK(cuMemsetD32(d1, 0, numThrs));
+  unsigned reps = (unsigned)numRepeats, sharers = (unsigned)numSharers, nc = numCounters, ng = numGroups,
+           pg = perGroup;
+  void* args[] = {&c0, &c1, &d0, &d1, &reps, &sharers, &nc, &ng, &pg};
+  CUevent e0, e1;
+  CK(cuEventCreate(&e0, CU_EVENT_DEFAULT));
+  CK(cuEventCreate(&e1, CU_EVENT_DEFAULT));
+  CK(cuEventRecord(e0, 0));
+  CK(cuLaunchKernel(fn, numTBs, 1, 1, tbSize, 1, 1, 0, 0, args, nullptr));
+  CK(cuEventRecord(e1, 0));
+  CK(cuEventSynchronize(e1));
+  CK(cuEventElapsedTime(elapsed_ms, e0, e1));
+  CK(cuMemcpyDtoH(counters0, c0, (size_t)numCounters * 4));
+  CK(cuMemcpyDtoH(counters1, c1, (size_t)numCounters * 4));
+  CK(cuMemcpyDtoH(del0, d0, (size_t)numThrs * 4));
+  CK(cuMemcpyDtoH(del1, d1, (size_t)numThrs * 4));
+  cuEventDestroy(e0);
+  cuEventDestroy(e1);
+  cuMemFree(c0);
+  cuMemFree(c1);
+  cuMemFree(d0);
+  cuMemFree(d1);
+  return 0;
+}

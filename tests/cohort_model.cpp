@@ -10,7 +10,7 @@
 // final state of every lock word.  Test code only.
 //
 //   cohort_model tas|ticket <threads> <iters> <max_pass> <local_wrap> <global_wrap>
-//   cohort_model sem <threads> <iters> <max_pass> <readers> <N>
+//   cohort_model sem <threads> <iters> <max_pass> <readers> <N> [local_wrap]
 // prints "ok <counter>" or "FAIL <reason>" and exits 0 / 1.
 #include <atomic>
 #include <cstdint>
@@ -115,19 +115,13 @@ std::atomic<unsigned long long> reader_ops{0};
 u32 kMaxc = 2;
 
 void sem_writer_thread(int me, int die, int iters) {
-  std::atomic<u32>& local = l_word[die];
   for (int i = 0; i < iters; ++i) {
-    local.fetch_add(1u << 16, std::memory_order_relaxed);
-    u32 got;
-    for (;;) {
-      u32 v = local.load(std::memory_order_relaxed);
-      if (v & 1u) continue;
-      if (local.compare_exchange_weak(v, (v | 1u) - (1u << 16), std::memory_order_acquire)) {
-        got = v;
-        break;
-      }
+    const u32 my = atom_inc(l_ticket[die], kLocalWrap);
+    u32 cur;
+    while (((cur = l_turn[die].load(std::memory_order_acquire)) >> 6) != my) {
     }
-    const u32 pc = (got >> 1) & 0x7FFFu, others = (got >> 16) - 1u;
+    const u32 pc = cur & 63u;
+    const u32 snap = l_ticket[die].load(std::memory_order_relaxed);
     if (pc == 0u) {  // take the semaphore by the writer rule
       for (;;) {
         u32 s = sem.load(std::memory_order_relaxed);
@@ -141,11 +135,12 @@ void sem_writer_thread(int me, int die, int iters) {
     if (writers_in.fetch_add(1) != 0 || readers_in.load() != 0) bad = true;
     critical_section(me);
     if (readers_in.load() != 0 || writers_in.fetch_sub(1) != 1) bad = true;
-    if (others != 0u && pc + 1u < kMaxPass) {
-      local.fetch_add(1u, std::memory_order_release);
+    const u32 next = (my >= kLocalWrap) ? 0u : my + 1u;
+    if (snap != next && pc + 1u < kMaxPass) {
+      l_turn[die].store((next << 6) | (pc + 1u), std::memory_order_release);
     } else {
       sem.fetch_add(kMaxc, std::memory_order_release);
-      local.fetch_add(0u - (2u * pc + 1u), std::memory_order_release);
+      l_turn[die].store(next << 6, std::memory_order_release);
     }
   }
 }
@@ -167,7 +162,7 @@ void sem_reader_thread(int, int, int iters) {
 }  // namespace
 
 int main(int argc, char** argv) {
-  if (argc != 7) {
+  if (argc != 7 && !(argc == 8 && std::strcmp(argv[1], "sem") == 0)) {
     std::fprintf(stderr, "usage: cohort_model tas|ticket threads iters max_pass local_wrap global_wrap\n"
                          "       cohort_model sem threads iters max_pass readers N\n");
     return 2;
@@ -176,11 +171,14 @@ int main(int argc, char** argv) {
   const int n = std::atoi(argv[2]), iters = std::atoi(argv[3]);
   if (std::strcmp(argv[1], "sem") == 0) {
     kMaxPass = (u32)std::atoi(argv[4]);
+    if (argc > 7) kLocalWrap = (u32)std::strtoul(argv[7], nullptr, 10);
     const int readers = std::atoi(argv[5]);
     kMaxc = (u32)std::atoi(argv[6]) + 1u;
     sem = kMaxc;
-    l_word[0] = 0;
-    l_word[1] = 0;
+    for (int d = 0; d < 2; ++d) {
+      l_ticket[d] = 0;
+      l_turn[d] = 0;
+    }
     std::vector<std::thread> ts;
     for (int t = 0; t < n; ++t) ts.emplace_back(sem_writer_thread, t, t % 2, iters);
     for (int t = 0; t < readers; ++t) ts.emplace_back(sem_reader_thread, n + t, 0, iters);
@@ -191,7 +189,8 @@ int main(int argc, char** argv) {
     if (reader_ops.load() != (unsigned long long)readers * iters) return std::puts("FAIL reader count"), 1;
     if (sem.load() != kMaxc) return std::printf("FAIL semaphore word %#x at the end\n", sem.load()), 1;
     for (int d = 0; d < 2; ++d)
-      if (l_word[d].load() != 0u) return std::printf("FAIL local word %d = %#x at the end\n", d, l_word[d].load()), 1;
+      if ((l_turn[d].load() >> 6) != l_ticket[d].load() || (l_turn[d].load() & 63u) != 0u)
+        return std::printf("FAIL die %d ticket %u turn %#x at the end\n", d, l_ticket[d].load(), l_turn[d].load()), 1;
     std::printf("ok %llu\n", counter);
     return 0;
   }

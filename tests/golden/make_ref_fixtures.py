@@ -6,6 +6,13 @@ Run on a GPU machine:  python tests/golden/make_ref_fixtures.py OUT.json
 The CPU test test_ref_fixtures_cpu.py recomputes the oracle golden for each
 entry and compares digests, pinning the oracle to the reference itself.
 Initial storage is the reference's storage[i] = i (as float).
+
+    python tests/golden/make_ref_fixtures.py relaxed OUT.json
+records the reference's own refCounter kernel (oracle/_ref/refcounter_sm100.cubin)
+for the sizes of REFCOUNTER_CASES: digests of both final counter arrays (the
+deterministic output) and whether each delete-flag array has a set entry (the
+reference's own check, refCounter.cu:86-120; which entries are set depends on
+the interleaving).
 """
 import hashlib
 import json
@@ -33,6 +40,26 @@ CASES = [
 ]
 
 
+# (numSharersPerGroup, numTBs, tbSize, numRepeats): the reference's own run
+# arguments (refCounter/run) first, then other sharing and sizes
+REFCOUNTER_CASES = [(32, 64, 32, 4), (1, 8, 256, 3), (4, 152, 128, 2), (2, 16, 64, 10), (8, 608, 256, 1)]
+
+
+def main_relaxed(out):
+    entries = []
+    for sharers, tbs, tb_size, reps in REFCOUNTER_CASES:
+        c0, c1, d0, d1, ms = oracle.ref_refcounter(sharers, tbs, tb_size, reps)
+        entries.append({"num_sharers": sharers, "num_tbs": tbs, "tb_size": tb_size, "num_repeats": reps,
+                        "counters": int(c0.size), "sha256_counters0": hashlib.sha256(c0.tobytes()).hexdigest(),
+                        "sha256_counters1": hashlib.sha256(c1.tobytes()).hexdigest(),
+                        "del0_any": bool(d0.any()), "del1_any": bool(d1.any()), "ref_ms": ms})
+        print("refCounter", sharers, tbs, tb_size, reps, "ok %.3f ms" % ms, flush=True)
+    with open(out, "w") as f:
+        json.dump({"generator": "tests/golden/make_ref_fixtures.py relaxed",
+                   "kernel": "refCounter_kernel (cuda/relaxedAtomics/uvm/refCounter), one launch",
+                   "entries": entries}, f, indent=1)
+
+
 def main(out):
     nsm, _ = oracle.ref_device()
     entries = []
@@ -52,4 +79,7 @@ def main(out):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(os.path.dirname(__file__), "ref_syncprims.json"))
+    if len(sys.argv) > 1 and sys.argv[1] == "relaxed":
+        main_relaxed(sys.argv[2] if len(sys.argv) > 2 else os.path.join(os.path.dirname(__file__), "ref_relaxed.json"))
+    else:
+        main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(os.path.dirname(__file__), "ref_syncprims.json"))

@@ -1,7 +1,7 @@
 """The cohort (die-aware) protocols, modelled on the host: std::threads stand
 for TBs on two dies and run the device code's encodings (test-and-set with
 waiters and passes in one word; ticket with the pass count in the turn word;
-semaphore writers as test-and-set cohorts over the packed semaphore word, with
+semaphore writers as ticket cohorts over the packed semaphore word, with
 readers beside them).  Small ticket wraps and pass limits drive the
 wrap-around and global release branches.  Mutual exclusion must hold (for the
 semaphore: no reader beside a writer, at most N readers), every critical
@@ -42,13 +42,13 @@ def test_cohort_protocol(model, kind, threads, iters, max_pass, lwrap, gwrap):
     assert p.returncode == 0 and p.stdout.startswith("ok %d" % (threads * iters)), p.stdout + p.stderr
 
 
-@pytest.mark.parametrize("writers,iters,max_pass,readers,n", [
-    (4, 20000, 32, 4, 1),     # the device's pass limit, semaphore of 1
-    (6, 10000, 2, 3, 2),      # frequent global posts
-    (5, 10000, 1, 6, 10),     # never passes
-    (8, 5000, 32, 0, 120),    # writers only (numTBs <= NUM_SM: every TB a writer)
+@pytest.mark.parametrize("writers,iters,max_pass,readers,n,lwrap", [
+    (4, 20000, 32, 4, 1, (1 << 25) - 1),  # the device's pass limit and ticket wrap, semaphore of 1
+    (6, 10000, 2, 3, 2, 7),               # frequent global posts, tickets wrap constantly
+    (5, 10000, 1, 6, 10, 5),              # never passes
+    (8, 5000, 32, 0, 120, 4),             # writers only (numTBs <= NUM_SM: every TB a writer)
 ])
-def test_cohort_semaphore_writers(model, writers, iters, max_pass, readers, n):
-    p = subprocess.run([model, "sem", str(writers), str(iters), str(max_pass), str(readers), str(n)],
+def test_cohort_semaphore_writers(model, writers, iters, max_pass, readers, n, lwrap):
+    p = subprocess.run([model, "sem", str(writers), str(iters), str(max_pass), str(readers), str(n), str(lwrap)],
                        capture_output=True, text=True, timeout=120)
     assert p.returncode == 0 and p.stdout.startswith("ok %d" % (writers * iters)), p.stdout + p.stderr

@@ -69,3 +69,18 @@ def test_reference_runner_refuses_global_semaphores(oracle, prim):
     init = np.zeros(oracle.storage_words(prim, 32, 2, 4, 152), dtype=np.uint32)
     with pytest.raises(RuntimeError, match="maxSemCount"):
         oracle.ref_run(prim, 32, 2, 4, 1, 1, init)
+
+
+@pytest.mark.parametrize("case", [(32, 64, 32, 4), (1, 8, 256, 3), (4, 152, 128, 2), (2, 16, 64, 10)])
+def test_reference_refcounter_matches_build(hs, oracle, case):
+    """refCounter: the reference's own kernel (one launch, refCounter.cu:24-82)
+    and this build leave the same final counters (all references dropped), and
+    both set delete flags (refCounter.cu:86-120)."""
+    import os
+    if not os.path.exists(oracle.ref_refcounter_module()):
+        pytest.skip("reference refCounter module not present")
+    sharers, tbs, tb_size, reps = case
+    r0, r1, rd0, rd1, _ = oracle.ref_refcounter(sharers, tbs, tb_size, reps)
+    c0, c1, d0, d1, _ = hs.refcounter(sharers, tbs, tb_size, reps)
+    assert np.array_equal(c0, r0) and np.array_equal(c1, r1)
+    assert rd0.any() and rd1.any() and d0.any() and d1.any()
