@@ -514,9 +514,13 @@ def uts_geo_extra(hs):
 
 def serve_extra(hs):
     """Served request loop: 256 requests from the mixed-instance generator
-    (numCSIters / 50), 64 slots of 8-CTA clusters; peak request rate, then
-    Poisson arrivals at 10-90% of it; p50/p99 latency from each request's due
-    time; the offline batch of the same requests; every result bit-exact."""
+    (numCSIters / 50, every eighth a tree search), 64 slots of 8-CTA clusters;
+    each request's latency alone, the burst rate, the sustainable peak (the
+    highest Poisson rate the open-loop driver keeps up with), then Poisson
+    arrivals at 10-90% of that peak: arrived and completed rates, p50/p99
+    latency from each request's due time, and slowdown (latency over latency
+    alone) overall and per request class; the offline batch of the same
+    requests; every result bit-exact."""
     from heterosync_gb300.served import served_sweep
     r = served_sweep(seed=SEED, n=256, iter_div=50, slots=64, gang=8)
     if not r["bit_exact"]:

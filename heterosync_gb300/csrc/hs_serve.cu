@@ -8,8 +8,10 @@
 //      (the project's fetch-and-add mutex, ticket_lock in hs_device.cuh) it
 //      takes the oldest pending request if the device arena has room for its
 //      storage and lock state -- admission is gated by free device memory, in
-//      arrival order; a request that does not fit waits until running
-//      requests release pages;
+//      arrival order; while the oldest does not fit, a later one (within 32
+//      entries) that fits may go first, until the oldest has waited 20 ms --
+//      then it waits for running requests to release pages and nothing
+//      passes it;
 //   2. the slot's CTAs copy the request's storage in from the pinned staging
 //      pool and lay out its lock state (zeroed words, semaphore counts, ring
 //      slots) in the request's pages;
@@ -93,7 +95,16 @@ struct ServeCtl {  // device memory
   unsigned long long a_head, a_tail;      // arena ring allocator (pages)
   unsigned long long rec_head, rec_tail;  // live allocations, oldest first
   unsigned status[2];
+  unsigned long long wait_req, wait_t0;   // the head request that did not fit (+1; 0: none) and since when
+  unsigned char taken[kServeQ];           // ring entries past qhead already admitted out of order
 };
+
+// Admission past a head request that does not fit: a later request within
+// kBypassWindow entries that fits is admitted first, but only while the head
+// has waited less than kBypassAgeNs -- after that nothing passes it, running
+// requests free their pages, and the head goes in: no request starves.
+constexpr unsigned kBypassWindow = 32;
+constexpr unsigned long long kBypassAgeNs = 20000000ull;
 
 enum : int { CMD_IDLE = 0, CMD_RUN = 1, CMD_STOP = 2, CMD_REJECT = 3, CMD_WAIT = 4 };
 
@@ -258,28 +269,54 @@ __device__ int serve_admit(const ServeArgs& a, SlotBox* box, const HsEnv& env) {
       if (!ticket_lock<GPU>(a.ctl->lock, a.ctl->lock + kLineWords, kTicketWrap, 0u, 0u, env)) return CMD_STOP;
       if (is_master()) {
         ServeCtl* c = a.ctl;
-        const unsigned long long head = c->qhead;
+        unsigned long long head = c->qhead;
         const unsigned long long tail = ld_acquire_sys64(&a.hctl->tail);
-        int r = CMD_IDLE;
-        if (head < tail) {
-          const ServeDesc* q = a.ring + (head % kServeQ);
+        while (head < tail && c->taken[head % kServeQ]) {  // skip entries admitted out of order
+          c->taken[head % kServeQ] = 0;
+          ++head;
+        }
+        c->qhead = head;
+        // request k: run it if the arena has room, reject it if it never fits
+        auto take = [&](unsigned long long k) {
+          const ServeDesc* q = a.ring + (k % kServeQ);
           const unsigned long long need = ld_relaxed_sys64(&q->pages);
           unsigned long long rec = 0;
+          int rr = CMD_WAIT;
           if (need == 0 || need > a.pages) {
-            r = CMD_REJECT;
+            rr = CMD_REJECT;
           } else {
             const long long page = arena_alloc(a, need, &rec);
             if (page >= 0) {
-              r = CMD_RUN;
+              rr = CMD_RUN;
               box->rec = rec;
               box->page = (unsigned long long)page;
-            } else {
-              r = CMD_WAIT;
             }
           }
+          if (rr != CMD_WAIT) box->req = k;
+          return rr;
+        };
+        int r = CMD_IDLE;
+        if (head < tail) {
+          r = take(head);
           if (r != CMD_WAIT) {
             c->qhead = head + 1;
-            box->req = head;
+          } else {
+            const unsigned long long now = globaltimer();
+            if (c->wait_req != head + 1) {
+              c->wait_req = head + 1;
+              c->wait_t0 = now;
+            }
+            if (now - c->wait_t0 < kBypassAgeNs) {
+              for (unsigned long long k = head + 1; k < tail && k < head + kBypassWindow; ++k) {
+                if (c->taken[k % kServeQ]) continue;
+                const int rk = take(k);
+                if (rk != CMD_WAIT) {
+                  c->taken[k % kServeQ] = 1;
+                  r = rk;
+                  break;
+                }
+              }
+            }
           }
         }
         s_cmd = r;

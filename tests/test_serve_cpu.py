@@ -26,3 +26,20 @@ def test_submit_without_server_is_rejected(hs):
     L = hs.lib()
     L.hs_serve_submit.argtypes = [ctypes.c_void_p] * 5
     assert L.hs_serve_submit(None, None, None, None, None) == 1
+
+
+def test_window_rates_ignore_the_drain():
+    """A server that keeps up completes requests as fast as they arrive inside
+    the middle of the arrival window, however long the last ones take; one that
+    falls behind completes fewer there than arrive."""
+    import numpy as np
+    from heterosync_gb300.served import poisson_arrivals, window_rates
+    arr = poisson_arrivals(1000.0, 4000, seed=3)
+    assert abs((len(arr) - 1) / arr[-1] - 1000.0) < 60
+    lat = np.full(arr.size, 2000.0)          # 2 ms each, constant: keeps up
+    lat[-5:] = 200000.0                      # a slow drain at the end does not count
+    arrived, completed = window_rates(arr, lat)
+    assert abs(completed / arrived - 1.0) < 0.01
+    behind = (np.arange(arr.size) / 500.0 - arr) * 1e6 + 2000.0   # completions at 500/s
+    arrived, completed = window_rates(arr, np.maximum(behind, 2000.0))
+    assert completed < 0.7 * arrived

@@ -159,3 +159,34 @@ def test_tree_search_requests_alone_and_in_mix(hs, oracle):
             k += 1
         else:
             assert np.array_equal(out, _expected(hs, x, a)), x
+
+
+def test_admission_passes_a_head_that_does_not_fit(hs):
+    """A large request that cannot fit while another large one runs does not
+    hold up small requests behind it: they are admitted past it (within the
+    admission window, before the head has waited 20 ms) and finish first; the
+    large one then runs once pages are free.  Every result is exact."""
+    nsm = hs.device_info()["nsm"]
+    long_run = (0, 40, 64, 3000)    # a tree barrier instance of ~2.7 MB, thousands of episodes
+    blocked = (0, 40, 64, 2)        # the same size: no room while the first one runs
+    smalls = [(7, 4, 4, 10), (4, 3, 6, 8), (20, 5, 8, 6), (10, 2, 4, 5)]
+    insts = [long_run, blocked] + smalls
+    rng = np.random.default_rng(11)
+    inits = [rng.integers(0, 1000, size=hs.Server.request_words(*x, nsm=nsm)).astype(np.uint32) for x in insts]
+    big = max(a.size for a in inits[:2]) * 4
+    # room for one large request and every small one, not for two large ones
+    arena = (big // (64 << 10) + 1 + 4 * 8) * (64 << 10)
+    srv = hs.Server(slots=4, gang=4, arena_bytes=arena, staging_bytes=64 << 20, idle_timeout_s=20.0)
+    try:
+        rid0, out0 = srv.submit(insts[0], inits[0])
+        time.sleep(0.002)  # the long request is admitted and holds its pages
+        ids = [(rid0, out0)] + [srv.submit(x, a) for x, a in zip(insts[1:], inits[1:])]
+        order = [c["id"] for c in srv.wait(len(insts))]
+        for k, (rid, out) in enumerate(ids):
+            assert np.array_equal(out, _expected(hs, insts[k], inits[k])), insts[k]
+        pos = {rid: i for i, rid in enumerate(order)}
+        small_ids = [rid for rid, _ in ids[2:]]
+        assert max(pos[r] for r in small_ids) < pos[ids[1][0]], order  # the small ones went past the blocked one
+        srv.stop()
+    finally:
+        srv.close()
