@@ -441,8 +441,17 @@ def batch_extra(hs):
     insts = hs.batch_generate(seed=SEED, n=64, iter_div=1)
     small = hs.batch_generate(seed=SEED, n=64, iter_div=25)
     tb = hs.Batch(small, mode="inc")
+    t0 = time.perf_counter()
     _, tune_ms = tb.autotune()
+    first = dict(tb.last_tune, wall_s=time.perf_counter() - t0)
     tuned = tb.tuned_settings()
+    tb.close()
+    tb = hs.Batch(small, mode="inc")   # the same batch again: its plan comes from the cache
+    t0 = time.perf_counter()
+    tb.autotune()
+    second = dict(tb.last_tune, wall_s=time.perf_counter() - t0)
+    if tb.tuned_settings() != tuned:
+        raise SystemExit("bench: the cached batch plan differs from the tuned one")
     tb.close()
     b = hs.Batch(insts, mode="inc")
     rng = np.random.default_rng(SEED)
@@ -471,8 +480,11 @@ def batch_extra(hs):
             "launches_per_instance_form": rs.launches, "batched_ms": round(rb.elapsed_ms, 2),
             "batched_ops_per_s": rb.ops / (rb.elapsed_ms * 1e-3), "ratio": rs.elapsed_ms / rb.elapsed_ms,
             "plan": {"cluster": tuned[0], "serial_executors": tuned[1], "tbs_per_executor": tuned[2],
-                     "stage_bytes": tuned[3], "backoff_max_ns": tuned[4], "grid": grid, "capacity": cap,
-                     "tuned_on": "numCSIters / 25 (%.1f ms)" % tune_ms}}
+                     "stage_bytes": tuned[3], "ctas_per_sm": {40 * 1024: 4, 56 * 1024: 3}.get(tuned[3]),
+                     "backoff_min_ns": tuned[5], "backoff_max_ns": tuned[4], "cta_threads": 256,
+                     "grid": grid, "capacity": cap,
+                     "tuned_on": "numCSIters / 25 (best trial %.1f ms)" % tune_ms,
+                     "cache": {"first": first, "second": second}}}
 
 
 def uts_geo_extra(hs):

@@ -763,6 +763,56 @@ def batch_generate(seed: int, n: int = 64, nsm: int = 0, iter_div: int = 1):
     return [(a.prim, a.num_ldst, a.num_tbs, a.num_iters) for a in arr]
 
 
+def plan_cache_path() -> str:
+    """Where tuned batch plans are kept: $HS_PLAN_CACHE, else
+    ~/.cache/heterosync_gb300/batch_plans.json."""
+    return os.environ.get("HS_PLAN_CACHE") or os.path.join(os.path.expanduser("~"), ".cache", "heterosync_gb300",
+                                                           "batch_plans.json")
+
+
+def plan_cache_key(instances, mode: str, device: Optional[dict] = None) -> str:
+    """A batch's cache key: the instances (kind, numLdSt, numTBs, numCSIters),
+    the data mode and the device (SM count, compute capability, max threads per
+    block); a plan tuned for one of them says nothing about another."""
+    import hashlib
+    import json
+    dev = device if device is not None else device_info()
+    blob = json.dumps({"instances": [list(map(int, x)) for x in instances], "mode": mode,
+                       "device": [int(dev["nsm"]), int(dev["cc"][0]), int(dev["cc"][1]),
+                                  int(dev["max_threads_per_block"])], "plan_format": 1}, sort_keys=True)
+    return hashlib.sha256(blob.encode()).hexdigest()
+
+
+def plan_cache_load(path: str, key: str):
+    import json
+    try:
+        with open(path) as f:
+            return json.load(f).get(key)
+    except (OSError, ValueError):
+        return None
+
+
+def plan_cache_store(path: str, key: str, entry: dict) -> None:
+    """Add one plan to the cache file (written to a temporary file and renamed,
+    so a reader never sees half a file)."""
+    import json
+    import tempfile
+    try:
+        os.makedirs(os.path.dirname(path) or ".", exist_ok=True)
+        try:
+            with open(path) as f:
+                data = json.load(f)
+        except (OSError, ValueError):
+            data = {}
+        data[key] = entry
+        fd, tmp = tempfile.mkstemp(dir=os.path.dirname(path) or ".", suffix=".tmp")
+        with os.fdopen(fd, "w") as f:
+            json.dump(data, f, indent=1)
+        os.replace(tmp, path)
+    except OSError:
+        pass  # an unwritable cache only costs the next run its trials
+
+
 class Batch:
     """Instances run in one persistent, graph-replayed launch (run) or one
     standalone launch each (run_serial)."""
@@ -846,15 +896,17 @@ class Batch:
         return int(lib().hs_batch_get_stage(self.h))
 
     def tuned_settings(self):
-        """(cluster, serial executors, v, staging bytes, backoff cap) of the current plan."""
+        """(cluster, serial executors, v, staging bytes, backoff cap, backoff start) of the current plan."""
         cl, se, v, _ = self.get_plan()
-        return cl, se, v, self.get_stage(), self.get_backoff()[1]
+        bo_min, bo_max = self.get_backoff()
+        return cl, se, v, self.get_stage(), bo_max, bo_min
 
     def apply_settings(self, settings):
         """Apply tuned_settings() of another batch (e.g. one tuned on fewer iterations)."""
-        cl, se, v, stage, bo = settings
+        cl, se, v, stage, bo = settings[:5]
+        bo_min = settings[5] if len(settings) > 5 else 1
         self.set_stage(stage)
-        self.set_backoff(1, bo)
+        self.set_backoff(bo_min, bo)
         return self.plan_ex(cl, se, v)
 
     def set_stage(self, nbytes: int):
@@ -862,9 +914,26 @@ class Batch:
         lib().hs_batch_set_stage.argtypes = [ctypes.c_void_p, ctypes.c_uint]
         self._check(lib().hs_batch_set_stage(self.h, nbytes))
 
-    def autotune(self):
+    def autotune(self, cache: Optional[str] = ""):
+        """Choose the launch plan (hs_batch_autotune) and apply it; returns
+        (v, ms of the best trial).  The plan is kept in a cache file keyed by
+        the instances, the data mode and the device (plan_cache_path(); None
+        disables it): a batch tuned before on this device gets its plan back
+        without any trial.  self.last_tune tells which happened."""
+        path = plan_cache_path() if cache == "" else cache
+        key = plan_cache_key(self.instances, self.mode) if path else None
+        if path:
+            hit = plan_cache_load(path, key)
+            if hit is not None:
+                s, _, _ = self.apply_settings(hit["settings"])
+                if s == 0:
+                    self.last_tune = {"cache": "hit", "path": path, "key": key[:16]}
+                    return self.get_plan()[2], float(hit["ms"])
         v, ms = ctypes.c_int(), ctypes.c_float()
         self._check(lib().hs_batch_autotune(self.h, None, ctypes.byref(v), ctypes.byref(ms)))
+        self.last_tune = {"cache": "miss" if path else "off", "path": path, "key": key[:16] if key else None}
+        if path:
+            plan_cache_store(path, key, {"settings": list(self.tuned_settings()), "ms": float(ms.value)})
         return v.value, ms.value
 
     def run(self):

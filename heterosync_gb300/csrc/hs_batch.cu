@@ -652,10 +652,12 @@ extern "C" int hs_batch_set_stage(hs_batch* B, unsigned bytes) {
 extern "C" unsigned hs_batch_get_stage(hs_batch* B) { return B ? B->stage : 0u; }
 
 // Autotuner: for staging sizes 40 and 56 KB (four or three CTAs per SM),
-// cluster sizes 1, 4, 8 and 8 to 32 executors for the heaviest serialised
+// cluster sizes 1, 2, 4, 8 and 8 to 32 executors for the heaviest serialised
 // instance, take the smallest v (1, 2, 4, ...) whose gangs fit, time one replay
-// on a copy of the initial storage and keep the fastest plan; then try
-// exponential-backoff caps of 256 and 32 ns against the default 1024.
+// on a copy of the initial storage and keep the fastest plan; then, for that
+// plan, the exponential-backoff bounds: start (I_min) 1, 8 or 64 ns and cap
+// (I_max) 1024, 256 or 32 ns.  The executor CTA stays one logical TB of 256
+// threads: its critical sections split their work by the TB's own threads.
 extern "C" int hs_batch_autotune(hs_batch* B, void* stream, int* best_v, float* best_ms) {
   if (!B) return HS_EINVAL;
   std::vector<std::vector<uint32_t>> saved(B->n);
@@ -678,7 +680,7 @@ extern "C" int hs_batch_autotune(hs_batch* B, void* stream, int* best_v, float* 
   // heaviest serialised instance; smallest v that fits
   for (unsigned stage : {40u * 1024u, 56u * 1024u}) {
     if (hs_batch_set_stage(B, stage) != HS_OK) continue;
-    for (int cl : {1, 4, 8}) {
+    for (int cl : {1, 2, 4, 8}) {
       for (int se : {8, 16, 32}) {
         int v = 1;
         while (v <= max_g && hs_batch_plan_ex(B, cl, se, v, nullptr, nullptr) != HS_OK) v *= 2;
@@ -689,15 +691,20 @@ extern "C" int hs_batch_autotune(hs_batch* B, void* stream, int* best_v, float* 
     }
   }
   if (!bcl) { g_berr = "no plan fits"; return HS_ENORES; }
-  // exponential-backoff cap for the winner
+  // exponential-backoff start and cap for the winner (the default 1 / 1024 was timed above)
   hs_batch_set_stage(B, bstage);
-  for (unsigned bo : {256u, 32u}) {
-    hs_batch_set_backoff(B, 1u, bo);
-    if (hs_batch_plan_ex(B, bcl, bse, bv, nullptr, nullptr) != HS_OK) continue;
-    const float t = trial();
-    if (t < best_t) { best_t = t; bbo = bo; }
+  const unsigned timed_min = B->bo_min, timed_max = B->bo_max;  // the bounds the plans above ran with
+  unsigned bmin = timed_min;
+  for (unsigned cap : {1024u, 256u, 32u}) {
+    for (unsigned lo : {1u, 8u, 64u}) {
+      if (lo >= cap || (lo == timed_min && cap == timed_max)) continue;
+      if (hs_batch_set_backoff(B, lo, cap) != HS_OK) continue;
+      if (hs_batch_plan_ex(B, bcl, bse, bv, nullptr, nullptr) != HS_OK) continue;
+      const float t = trial();
+      if (t < best_t) { best_t = t; bbo = cap; bmin = lo; }
+    }
   }
-  hs_batch_set_backoff(B, 1u, bbo);
+  hs_batch_set_backoff(B, bmin, bbo);
   hs_batch_plan_ex(B, bcl, bse, bv, nullptr, nullptr);
   if (best_v) *best_v = bv;
   if (best_ms) *best_ms = best_t;

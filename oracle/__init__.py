@@ -43,6 +43,12 @@ def lib() -> ctypes.CDLL:
         L.hs_oracle_storage_words.restype = ctypes.c_long
         L.hs_oracle_golden.argtypes = [ctypes.c_int] * 8 + [ctypes.c_void_p, ctypes.c_long]
         L.hs_oracle_slice.argtypes = [ctypes.c_int] * 6 + [ctypes.c_void_p, ctypes.c_long]
+        # pointers always as void*: without argtypes ctypes passes a Python int as a 32-bit C int
+        L.hs_oracle_uts_tree.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint, ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.hs_oracle_uts_frontier.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_void_p]
+        L.hs_oracle_storage_words.restype = ctypes.c_long
         _lib = L
     return _lib
 
@@ -176,7 +182,7 @@ def uts_tree(num_nodes: int, fertility: int, seed: int = 200):
     L_ = lib()
     tree = np.zeros(num_nodes, dtype=UTS_NODE)
     lv, ls, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint()
-    rc = L_.hs_oracle_uts_tree(num_nodes, fertility, ctypes.c_uint(seed), tree.ctypes.data, ctypes.byref(lv),
+    rc = L_.hs_oracle_uts_tree(num_nodes, fertility, seed, tree.ctypes.data, ctypes.byref(lv),
                                ctypes.byref(ls), ctypes.byref(rs))
     if rc:
         raise ValueError("bad UTS tree size")

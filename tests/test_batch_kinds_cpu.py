@@ -70,3 +70,25 @@ def test_syncprims_expected_matches_run_config_form(hs):
         cfg = hs.RunConfig(prim=p, num_ldst=L, num_tbs=G, num_iters=I, threads=256, repeats=1, mode="inc", nsm=NSM)
         init = _init(hs.storage_words(cfg), p)
         assert np.array_equal(hs.batch_expected(x, init, NSM), hs.expected_storage(cfg, init, NSM))
+
+
+def test_plan_cache_keys_and_round_trip(tmp_path):
+    """Tuned batch plans are cached per (instances, mode, device): the key
+    changes with any of them; a stored plan reads back; a missing or broken
+    file reads as no plan."""
+    import heterosync_gb300 as hs
+    dev = {"nsm": 152, "cc": (10, 3), "max_threads_per_block": 1024}
+    insts = [(4, 10, 8, 100), (62, 4, 32, 5)]
+    k = hs.plan_cache_key(insts, "inc", dev)
+    assert k == hs.plan_cache_key([tuple(x) for x in insts], "inc", dict(dev))
+    assert k != hs.plan_cache_key(insts, "ref", dev)
+    assert k != hs.plan_cache_key(insts[:1], "inc", dev)
+    assert k != hs.plan_cache_key(insts, "inc", dict(dev, nsm=148))
+    path = str(tmp_path / "sub" / "plans.json")
+    assert hs.plan_cache_load(path, k) is None
+    hs.plan_cache_store(path, k, {"settings": [8, 8, 32, 57344, 1024, 1], "ms": 12.5})
+    hs.plan_cache_store(path, "other", {"settings": [1, 16, 128, 57344, 32, 8], "ms": 3.0})
+    assert hs.plan_cache_load(path, k) == {"settings": [8, 8, 32, 57344, 1024, 1], "ms": 12.5}
+    with open(path, "w") as f:
+        f.write("{not json")
+    assert hs.plan_cache_load(path, k) is None

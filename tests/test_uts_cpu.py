@@ -64,3 +64,16 @@ def test_frontier_matches_oracle(hs, oracle, cores):
 def test_even_tree_size_rejected(hs):
     with pytest.raises(hs.HsError):
         hs.uts_tree(100, 90, 200)
+
+
+def test_large_tree_builders_agree(hs, oracle):
+    """A 262,145-node tree (5 MB of nodes, allocated where a pointer no longer
+    fits 32 bits): the oracle's generator and the library's host builder give
+    the same tree and the same golden counts."""
+    import numpy as np
+    tree, leaves, leaf_sum, restarts = oracle.uts_tree(262145, 70, 200)
+    mine, l2, s2, r2 = hs.uts_tree(262145, 70, 200)
+    assert (leaves, leaf_sum, restarts) == (l2, s2, r2)
+    assert np.array_equal(tree["child_a"], mine["child_a"]) and np.array_equal(tree["value"], mine["value"])
+    fr, proc = oracle.uts_frontier(tree, 15)
+    assert len(fr) == 15 * 16 and proc > 0
