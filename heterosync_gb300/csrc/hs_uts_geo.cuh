@@ -221,9 +221,35 @@ struct GeoFrame {
   int next, end;
 };
 
+// Work count of this side: every lane of the warp adds its change (a lane
+// that received a subtree from a warp-mate: +1; a lane whose subtree is done:
+// -1) and lane 0 applies the warp's sum with one atomic.  A subtree handed over
+// inside a warp stays counted through its donor, so the count never passes
+// through zero while work is left.
+template <bool COOP>
+static __device__ __forceinline__ void geo_work_delta(const GeoArgs& a, int delta) {
+  const int sum = __reduce_add_sync(0xFFFFFFFFu, delta);
+  if ((threadIdx.x & 31u) == 0u && sum != 0) {
+    if constexpr (COOP) {
+      const unsigned old = atom_add_acqrel<GPU>(a.work, (unsigned)sum);
+      if (sum < 0 && old + (unsigned)sum == 0u) atom_add_acqrel<SYS>(a.br.ctl, 0xFFFFFFFFu);  // the side went idle
+    } else {
+      asm volatile("red.release.gpu.global.add.u32 [%0], %1;" :: "l"(a.work), "r"((unsigned)sum) : "memory");
+    }
+  }
+  __syncwarp();  // the warp's count change is ordered before its lanes' next reads of the count
+}
+
 // The walk, run by every thread of the walking CTAs (rank = this CTA's index
-// among them): the standalone kernel's grid, or a server slot's CTAs.  Each
-// CTA pushes to queue rank % nq and steals from random others.
+// among them): the standalone kernel's grid, or a server slot's CTAs.
+//
+// Each lane walks its own subtrees depth first (a stack of frames), 16 nodes
+// per round.  The warp stays converged: after every round, lanes with nothing
+// left receive the upper half of the oldest frame of a warp-mate that has two
+// or more children left there, through shuffles (no global memory, no
+// atomics); only lanes the warp cannot feed go to the CTA queues (own queue
+// first, then random victims).  Busy lanes give work to those queues while
+// threads anywhere are idle.  Each CTA pushes to queue rank % nq.
 //
 // COOP: host threads walk the same tree (hs_uts_geo.cu).  A busy thread gives
 // host walkers that are idle a subtree near the depth limit (3 to 7 levels
@@ -236,6 +262,7 @@ struct GeoFrame {
 template <bool COOP = false>
 static __device__ void uts_geo_walk(const GeoArgs& a, unsigned rank) {
   constexpr unsigned long long kPollNs = 16000;  // a poll costs a few link round trips
+  constexpr unsigned kFull = 0xFFFFFFFFu;
   __shared__ unsigned s_t[kGeoTable];
   __shared__ unsigned s_poll;
   __shared__ unsigned long long s_poll_t;
@@ -247,6 +274,7 @@ static __device__ void uts_geo_walk(const GeoArgs& a, unsigned rank) {
   __syncthreads();
   const HsEnv env{a.status, a.timeout_ns};
   const int myq = (int)(rank % (unsigned)a.nq);
+  const unsigned lane = threadIdx.x & 31u, lanes_below = (1u << lane) - 1u;
   unsigned rng = 0x9E3779B9u * (rank * blockDim.x + threadIdx.x + 1u);
   GeoFrame st[kGeoMaxDepth + 1];
   int sp = 0;  // frames on the stack; frame f holds a node at depth base + f
@@ -276,14 +304,14 @@ static __device__ void uts_geo_walk(const GeoArgs& a, unsigned rank) {
       busy = true;
     }
   }
-  bool counted_idle = false;
+  bool counted_idle = false, stop = false;
   unsigned long long t0 = 0;
   unsigned last_work = 0;
   unsigned nap = 64;
   for (;;) {
+    int delta = 0;
     if (busy) {
-      // walk up to 64 nodes, then consider giving work away
-      for (int step = 0; step < 64 && sp > 0; ++step) {
+      for (int step = 0; step < 16 && sp > 0; ++step) {
         GeoFrame& f = st[sp - 1];
         if (f.next == f.end) {
           --sp;
@@ -306,130 +334,181 @@ static __device__ void uts_geo_walk(const GeoArgs& a, unsigned rank) {
           ++sp;
         }
       }
+      while (sp > 0 && st[sp - 1].next == st[sp - 1].end) --sp;
       if (sp == 0) {
         busy = false;
+        delta = -1;
+      } else {
         if constexpr (COOP) {
-          if (atom_add_acqrel<GPU>(a.work, 0xFFFFFFFFu) == 1u) atom_add_acqrel<SYS>(a.br.ctl, 0xFFFFFFFFu);
-        } else {
-          asm volatile("red.release.gpu.global.add.u32 [%0], %1;" :: "l"(a.work), "r"(0xFFFFFFFFu) : "memory");
-        }
-        continue;
-      }
-      if constexpr (COOP) {
-        if ((++batches & 15u) == 0u) {  // every 1024 nodes: heartbeat, and feed idle host walkers
-          if (threadIdx.x == 0) st_relaxed<SYS>(a.br.ctl + 192, (unsigned)(globaltimer() >> 16));
-          const unsigned hidle = ld_relaxed<SYS>(a.br.ctl + 32);
-          if (hidle != 0u && ld_relaxed<GPU>(a.br.dev) - ld_relaxed<SYS>(a.br.ctl + 128) < hidle) {
-            for (int f = 0; f < sp; ++f) {
-              const int left = st[f].end - st[f].next;
-              const int levels = a.limit - (int)(base + (unsigned)f);
-              if (left >= 2 && levels <= kHostLevels && levels >= kHostMinLevels) {
-                GeoItem it;
-                for (int k = 0; k < 5; ++k) it.s[k] = st[f].s[k];
-                it.depth = base + (unsigned)f;
-                it.first = (unsigned)(st[f].next + left / 2);
-                it.end = (unsigned)st[f].end;
-                atom_add_acqrel<SYS>(a.br.ctl, 1u);
-                if (g2h_push(a.br, it)) st[f].end = (int)it.first;
-                else atom_add_acqrel<SYS>(a.br.ctl, 0xFFFFFFFFu);
-                break;
+          if ((++batches & 63u) == 0u) {  // every 1024 nodes: heartbeat, and feed idle host walkers
+            if (threadIdx.x == 0) st_relaxed<SYS>(a.br.ctl + 192, (unsigned)(globaltimer() >> 16));
+            const unsigned hidle = ld_relaxed<SYS>(a.br.ctl + 32);
+            if (hidle != 0u && ld_relaxed<GPU>(a.br.dev) - ld_relaxed<SYS>(a.br.ctl + 128) < hidle) {
+              for (int f = 0; f < sp; ++f) {
+                const int left = st[f].end - st[f].next;
+                const int levels = a.limit - (int)(base + (unsigned)f);
+                if (left >= 2 && levels <= kHostLevels && levels >= kHostMinLevels) {
+                  GeoItem it;
+                  for (int k = 0; k < 5; ++k) it.s[k] = st[f].s[k];
+                  it.depth = base + (unsigned)f;
+                  it.first = (unsigned)(st[f].next + left / 2);
+                  it.end = (unsigned)st[f].end;
+                  atom_add_acqrel<SYS>(a.br.ctl, 1u);
+                  if (g2h_push(a.br, it)) st[f].end = (int)it.first;
+                  else atom_add_acqrel<SYS>(a.br.ctl, 0xFFFFFFFFu);
+                  break;
+                }
               }
             }
           }
         }
-      }
-      if (ld_relaxed<GPU>(a.idle) != 0u) {
-        // give away the upper half of the oldest frame with two or more children left
-        for (int f = 0; f < sp; ++f) {
-          const int left = st[f].end - st[f].next;
-          if (left >= 2) {
-            GeoItem it;
-            for (int k = 0; k < 5; ++k) it.s[k] = st[f].s[k];
-            it.depth = base + (unsigned)f;
-            it.first = (unsigned)(st[f].next + left / 2);
-            it.end = (unsigned)st[f].end;
-            atomicAdd(a.work, 1u);
-            if (q_push(a, myq, it)) st[f].end = (int)it.first;
-            else asm volatile("red.relaxed.gpu.global.add.u32 [%0], %1;" :: "l"(a.work), "r"(0xFFFFFFFFu) : "memory");
-            break;
+        if (ld_relaxed<GPU>(a.idle) != 0u) {
+          // threads elsewhere are idle: the upper half of the oldest frame with two or more children left
+          for (int f = 0; f < sp; ++f) {
+            const int left = st[f].end - st[f].next;
+            if (left >= 2) {
+              GeoItem it;
+              for (int k = 0; k < 5; ++k) it.s[k] = st[f].s[k];
+              it.depth = base + (unsigned)f;
+              it.first = (unsigned)(st[f].next + left / 2);
+              it.end = (unsigned)st[f].end;
+              atomicAdd(a.work, 1u);
+              if (q_push(a, myq, it)) st[f].end = (int)it.first;
+              else asm volatile("red.relaxed.gpu.global.add.u32 [%0], %1;" :: "l"(a.work), "r"(0xFFFFFFFFu) : "memory");
+              break;
+            }
           }
         }
       }
-      continue;
     }
-    // idle: own queue first, then a few random victims
-    GeoItem it;
-    bool got = q_pop(a, myq, it);
-    for (int v = 0; v < 4 && !got; ++v) {
-      rng ^= rng << 13; rng ^= rng >> 17; rng ^= rng << 5;
-      got = q_pop(a, (int)(rng % (unsigned)a.nq), it);
-    }
-    unsigned w = 0;
-    if constexpr (COOP) {
-      if (!got && ld_relaxed<GPU>(a.br.dev + 64) != 0u) break;  // done
-      const unsigned long long now = globaltimer();
-      if (!got && now - *(volatile unsigned long long*)&s_poll_t >= kPollNs && atomicCAS(&s_poll, 0u, 1u) == 0u) {
-        s_poll_t = now;
-        if (h2g_pop(a.br, it)) {
-          got = true;
-          // the item's share of the global count becomes this side's, unless the side was active already
-          if (atom_add_acqrel<GPU>(a.work, 1u) != 0u) atom_add_acqrel<SYS>(a.br.ctl, 0xFFFFFFFFu);
-        } else {
-          const unsigned g = ld_acquire<SYS>(a.br.ctl);
-          const unsigned ab = ld_relaxed<SYS>(a.br.ctl + 96);
-          if (g == 0u || ab != 0u) {
-            if (ab != 0u) fail(env, HS_DEV_TIMEOUT, HS_SITE_UTS);
-            st_release<GPU>(a.br.dev + 64, 1u);
-            atomicExch(&s_poll, 0u);
+    // hand-overs inside the warp: idle lanes take the upper half of a warp-mate's oldest divisible frame
+    const unsigned idle_m = __ballot_sync(kFull, !busy && !stop);
+    if (idle_m != 0u) {
+      int fd = -1;
+      if (busy)
+        for (int f = 0; f < sp; ++f)
+          if (st[f].end - st[f].next >= 2) {
+            fd = f;
             break;
           }
-          // ask the host walkers for work once more than half of this side's threads are idle
-          if (ld_relaxed<GPU>(a.work) < gridDim.x * blockDim.x / 2u && ld_relaxed<SYS>(a.br.ctl + 64) == 0u)
-            st_relaxed<SYS>(a.br.ctl + 64, 1u);
-          st_relaxed<GPU>(a.br.dev + 96, g * 0x9E3779B1u ^ ld_relaxed<SYS>(a.br.ctl + 224));
+      const unsigned donor_m = __ballot_sync(kFull, fd >= 0);
+      const int pairs = min(__popc(idle_m), __popc(donor_m));
+      if (pairs > 0) {
+        unsigned v[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+        if (fd >= 0) {
+          const int left = st[fd].end - st[fd].next;
+          for (int k = 0; k < 5; ++k) v[k] = st[fd].s[k];
+          v[5] = base + (unsigned)fd;
+          v[6] = (unsigned)(st[fd].next + left / 2);
+          v[7] = (unsigned)st[fd].end;
         }
-        atomicExch(&s_poll, 0u);
+        const int ir = __popc(idle_m & lanes_below), dr = __popc(donor_m & lanes_below);
+        const bool recv = ((idle_m >> lane) & 1u) && ir < pairs;
+        const int src = recv ? (int)__fns(donor_m, 0u, ir + 1) : (int)lane;
+        unsigned g[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) g[k] = __shfl_sync(kFull, v[k], src);
+        if (fd >= 0 && dr < pairs) st[fd].end = (int)v[6];  // a matched donor keeps the lower half
+        if (recv) {
+          for (int k = 0; k < 5; ++k) st[0].s[k] = g[k];
+          base = g[5];
+          st[0].next = (int)g[6];
+          st[0].end = (int)g[7];
+          sp = 1;
+          busy = true;
+          delta += 1;
+          nap = 64;
+          t0 = 0;
+          if (counted_idle) {
+            atomicSub(a.idle, 1u);
+            counted_idle = false;
+          }
+        }
       }
-      if (!got) w = ld_acquire<GPU>(a.work) ^ (ld_relaxed<GPU>(a.br.dev + 96) * 0x85EBCA77u);
     }
-    if (got) {
-      if (counted_idle) {
-        atomicSub(a.idle, 1u);
-        counted_idle = false;
+    geo_work_delta<COOP>(a, delta);
+    // lanes the warp could not feed: the CTA queues, then (cooperative) the host
+    const bool warp_idle = __all_sync(kFull, !busy);
+    if (!busy && !stop) {
+      GeoItem it;
+      bool got = q_pop(a, myq, it);
+      for (int v = 0; v < 4 && !got; ++v) {
+        rng ^= rng << 13; rng ^= rng >> 17; rng ^= rng << 5;
+        got = q_pop(a, (int)(rng % (unsigned)a.nq), it);
       }
-      for (int k = 0; k < 5; ++k) st[0].s[k] = it.s[k];
-      st[0].next = (int)it.first;
-      st[0].end = (int)it.end;
-      base = it.depth;
-      sp = 1;
-      busy = true;
-      nap = 64;
-      t0 = 0;
-      continue;
-    }
-    if (!counted_idle) {
-      atomicAdd(a.idle, 1u);
-      counted_idle = true;
-    }
-    if constexpr (!COOP) {
-      w = ld_acquire<GPU>(a.work);
-      if (w == 0u) break;
-    }
-    // bounded: the work count (and, cooperative, the host's view) must move within the time limit
-    const unsigned long long now = globaltimer();
-    if (t0 == 0 || w != last_work) {
-      t0 = now;
-      last_work = w;
-    } else if (now - t0 > a.timeout_ns || ld_relaxed<GPU>(a.status) != 0u) {
-      if (ld_relaxed<GPU>(a.status) == 0u) fail(env, HS_DEV_TIMEOUT, HS_SITE_UTS);
+      unsigned w = 0;
       if constexpr (COOP) {
-        st_relaxed<SYS>(a.br.ctl + 96, 1u);  // the host walkers stop too
-        st_release<GPU>(a.br.dev + 64, 1u);
+        if (!got && ld_relaxed<GPU>(a.br.dev + 64) != 0u) stop = true;  // done
+        const unsigned long long now = globaltimer();
+        if (!got && !stop && now - *(volatile unsigned long long*)&s_poll_t >= kPollNs &&
+            atomicCAS(&s_poll, 0u, 1u) == 0u) {
+          s_poll_t = now;
+          if (h2g_pop(a.br, it)) {
+            got = true;
+            // the item's share of the global count becomes this side's, unless the side was active already
+            if (atom_add_acqrel<GPU>(a.work, 1u) != 0u) atom_add_acqrel<SYS>(a.br.ctl, 0xFFFFFFFFu);
+          } else {
+            const unsigned gc = ld_acquire<SYS>(a.br.ctl);
+            const unsigned ab = ld_relaxed<SYS>(a.br.ctl + 96);
+            if (gc == 0u || ab != 0u) {
+              if (ab != 0u) fail(env, HS_DEV_TIMEOUT, HS_SITE_UTS);
+              st_release<GPU>(a.br.dev + 64, 1u);
+              stop = true;
+            } else {
+              // ask the host walkers for work once more than half of this side's threads are idle
+              if (ld_relaxed<GPU>(a.work) < gridDim.x * blockDim.x / 2u && ld_relaxed<SYS>(a.br.ctl + 64) == 0u)
+                st_relaxed<SYS>(a.br.ctl + 64, 1u);
+              st_relaxed<GPU>(a.br.dev + 96, gc * 0x9E3779B1u ^ ld_relaxed<SYS>(a.br.ctl + 224));
+            }
+          }
+          atomicExch(&s_poll, 0u);
+        }
+        if (!got && !stop) w = ld_acquire<GPU>(a.work) ^ (ld_relaxed<GPU>(a.br.dev + 96) * 0x85EBCA77u);
       }
-      break;
+      if (got) {  // a queue item's count passes to this lane (queued items and busy lanes are both counted)
+        if (counted_idle) {
+          atomicSub(a.idle, 1u);
+          counted_idle = false;
+        }
+        for (int k = 0; k < 5; ++k) st[0].s[k] = it.s[k];
+        st[0].next = (int)it.first;
+        st[0].end = (int)it.end;
+        base = it.depth;
+        sp = 1;
+        busy = true;
+        nap = 64;
+        t0 = 0;
+      } else if (!stop) {
+        if (!counted_idle) {
+          atomicAdd(a.idle, 1u);
+          counted_idle = true;
+        }
+        if constexpr (!COOP) {
+          w = ld_acquire<GPU>(a.work);
+          if (w == 0u) stop = true;
+        }
+        if (!stop) {
+          // bounded: the work count (and, cooperative, the host's view) must move within the time limit
+          const unsigned long long now = globaltimer();
+          if (t0 == 0 || w != last_work) {
+            t0 = now;
+            last_work = w;
+          } else if (now - t0 > a.timeout_ns || ld_relaxed<GPU>(a.status) != 0u) {
+            if (ld_relaxed<GPU>(a.status) == 0u) fail(env, HS_DEV_TIMEOUT, HS_SITE_UTS);
+            if constexpr (COOP) {
+              st_relaxed<SYS>(a.br.ctl + 96, 1u);  // the host walkers stop too
+              st_release<GPU>(a.br.dev + 64, 1u);
+            }
+            stop = true;
+          }
+          if (!stop && warp_idle) {  // only a warp with no busy lane waits
+            sleep_ns(nap);
+            nap = nap < 1024u ? nap * 2u : 1024u;
+          }
+        }
+      }
     }
-    sleep_ns(nap);
-    nap = nap < 1024u ? nap * 2u : 1024u;
+    if (__all_sync(kFull, stop)) break;
   }
   if (counted_idle) atomicSub(a.idle, 1u);
   atomicAdd(a.out, nodes);
