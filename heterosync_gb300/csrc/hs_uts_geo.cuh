@@ -311,12 +311,12 @@ static __device__ void uts_geo_walk(const GeoArgs& a, unsigned rank) {
   for (;;) {
     int delta = 0;
     if (busy) {
-      for (int step = 0; step < 16 && sp > 0; ++step) {
+      for (int step = 0; step < 16; ++step) {
+        // exhausted frames are popped first, so every lane with work left
+        // hashes in the same iteration (the SHA-1 rounds run with full warps)
+        while (sp > 0 && st[sp - 1].next == st[sp - 1].end) --sp;
+        if (sp == 0) break;
         GeoFrame& f = st[sp - 1];
-        if (f.next == f.end) {
-          --sp;
-          continue;
-        }
         unsigned c[5];
         geo_child(f.s, (unsigned)f.next, c);
         f.next += 1;
