@@ -691,9 +691,9 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c0, void* storage, int o
   d.grp = tbs_per_cta;
   r->cluster = cluster;
   r->tbs_per_cta = tbs_per_cta;
-  // global spin / FA mutex, or global semaphore (its writers), with more than
-  // one TB: the die-aware cohort form
-  if ((c->prim == 4 || c->prim == 7 || (c->prim >= 8 && c->prim <= 15)) && c->num_tbs > 1 && grid == c->num_tbs &&
+  // global mutex, or global semaphore (its writers), with more than one TB:
+  // the die-aware cohort form
+  if (c->prim >= 4 && c->prim <= 15 && c->num_tbs > 1 && grid == c->num_tbs &&
       !(c->flags & HS_RUN_NO_COHORT) && cohort_ready(ctx)) {
     d.cohort = 1;
     d.die_map = reinterpret_cast<const unsigned char*>(ctx->coh_pool);

@@ -33,25 +33,67 @@ template <int S, int KIND, int MODE, int V, bool TMA>
 __device__ __forceinline__ void mutex_loop(const RunDesc& d, int g, int r, int m, int G, unsigned* w0, unsigned* w1,
                                            unsigned* w2, unsigned* ring, unsigned ring_max, unsigned wrap,
                                            int* s_slot, TmaCtx& tma, const HsEnv& env) {
-  if constexpr (S == GPU && (KIND == MK_SPIN || KIND == MK_FA)) {
-    if (d.cohort) {  // global mutex as a cohort of per-die locks (hs_device.cuh)
+  if constexpr (S == GPU) {
+    if (d.cohort) {  // global mutex as a cohort of per-die ticket queues (hs_device.cuh)
       unsigned sm;
       asm volatile("mov.u32 %0, %%smid;" : "=r"(sm));
       const int die = d.die_map[sm & 255u] & 1;
       unsigned* const* c = d.coh + 3 * die;
-      unsigned my = 0, pc = 0, aux = 0;  // meaningful in the master thread
+      unsigned my = 0, pc = 0, aux = 0, slot = 0;  // meaningful in the master thread
       for (int j = 0; j < d.iters; ++j) {
         bool ok;
-        if constexpr (KIND == MK_FA)
+        if constexpr (KIND == MK_FA) {
           ok = cohort_ticket_lock(c[0], c[1], w0, w1, wrap, d.bo_unit, d.bo_max, env, my, pc, aux);
-        else
-          ok = cohort_tas_lock(c[0], w0, env, pc, aux);
+        } else if constexpr (KIND == MK_SLEEP) {
+          // the ring slot that holds the global lock travels with the passes (line 2)
+          ok = cohort_queue_lock(
+              c[0], c[1],
+              [&] {
+                slot = atom_inc_relaxed<GPU>(w2, ring_max);
+                unsigned* mine = ring + (size_t)slot * kRingStride;
+                unsigned* prev = ring + (size_t)(slot == 0u ? ring_max : slot - 1u) * kRingStride;
+                return wait_until_p([&] { return ld_acquire<GPU>(mine) == 1u; },
+                                    [&] { return ld_relaxed<GPU>(prev); }, [&] { sleep_ns(d.bo_unit); }, env,
+                                    HS_SITE_SLEEP_LOCK);
+              },
+              env, HS_SITE_SLEEP_LOCK, my, pc, aux);
+          if (is_master() && pc != 0u) slot = ld_relaxed<GPU>(c[2]);
+        } else {
+          ok = cohort_queue_lock(
+              c[0], c[1],
+              [&] {
+                unsigned b = d.bo_min;
+                return wait_until(
+                    [&] { return ld_relaxed<GPU>(w0) == 0u && atom_cas_acquire<GPU>(w0, 0u, 1u) == 0u; },
+                    [&] {
+                      if constexpr (KIND == MK_EBO) {
+                        sleep_ns(b);
+                        b = ebo_next(b, d.bo_max);
+                      }
+                    },
+                    env, KIND == MK_EBO ? HS_SITE_EBO_LOCK : HS_SITE_SPIN_LOCK);
+              },
+              env, KIND == MK_EBO ? HS_SITE_EBO_LOCK : HS_SITE_SPIN_LOCK, my, pc, aux);
+        }
         if (!ok) break;
         if constexpr (MODE == M_SLICE) cs_slice(d.data, g + ((r + j) % m) * G, d.L);
         else if constexpr (TMA) ok = cs_chunk_tma<MODE>(d, g, tma, env);
         else cs_chunk<MODE, V>(d, g);
-        if constexpr (KIND == MK_FA) cohort_ticket_unlock(c[1], w1, wrap, my, pc, aux);
-        else cohort_tas_unlock(c[0], w0, pc, aux);
+        if constexpr (KIND == MK_FA) {
+          cohort_ticket_unlock(c[1], w1, wrap, my, pc, aux);
+        } else if constexpr (KIND == MK_SLEEP) {
+          if (is_master()) st_relaxed<GPU>(c[2], slot);  // ordered before the pass by its release
+          cohort_queue_unlock(
+              c[1],
+              [&] {
+                const unsigned next = (slot >= ring_max) ? 0u : slot + 1u;
+                st_relaxed<GPU>(ring + (size_t)slot * kRingStride, 0xFFFFFFFFu);
+                st_release<GPU>(ring + (size_t)next * kRingStride, 1u);
+              },
+              my, pc, aux);
+        } else {
+          cohort_queue_unlock(c[1], [&] { st_release<GPU>(w0, 0u); }, my, pc, aux);
+        }
         if (!ok) break;
       }
       return;

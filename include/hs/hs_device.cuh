@@ -253,55 +253,14 @@ __device__ __forceinline__ void ticket_unlock(unsigned* turn, unsigned wrap) {
 // word costs ~450 ns, any hand-off that crosses the dies ~750 ns (and an
 // atomic ~150 against ~330 ns).  A cohort lock keeps hand-offs on one die: each
 // die has a local lock homed on it, and the global lock (the primitive's own
-// word) is taken only by a TB that did not inherit it.  A releasing holder
+// word) is taken only by a TB that did not inherit it.  The local lock is a
+// ticket queue whose turn word also counts the passes.  A releasing holder
 // with local waiters passes the local lock together with the global one, at
 // most kCohortMaxPass times in a row; otherwise it releases both.  Mutual
 // exclusion is the global lock's (held by one cohort) and the local lock's
 // (one holder in the cohort).
 // ---------------------------------------------------------------------------
 constexpr unsigned kCohortMaxPass = 32;
-
-// Test-and-set cohort: the local word packs [31:16] waiters, [15:1] passes so
-// far (0: the cohort does not hold the global lock), [0] held.  The global
-// word is a test-and-set lock.  The acquiring CAS returns the waiter count,
-// so the holder knows at acquisition whether anyone on its die waits (a
-// registered waiter keeps waiting until it holds the lock); the release is
-// then one red.release.add: +1 turns "held, pc" into "free, pc + 1" (pass),
-// -(2 pc + 1) into "free, 0" (after the global release).
-__device__ __forceinline__ bool cohort_tas_lock(unsigned* local, unsigned* global, const HsEnv& env, unsigned& pc,
-                                                unsigned& others) {
-  int ok = 0;
-  if (is_master()) {
-    atomicAdd(local, 1u << 16);  // register as a waiter
-    unsigned got = 0;
-    ok = wait_until(
-        [&] {
-          const unsigned v = ld_relaxed<GPU>(local);
-          if (v & 1u) return false;
-          if (atom_cas_acquire<GPU>(local, v, (v | 1u) - (1u << 16)) != v) return false;
-          got = v;
-          return true;
-        },
-        [] {}, env, HS_SITE_SPIN_LOCK);
-    pc = (got >> 1) & 0x7FFFu;
-    others = (got >> 16) - 1u;
-    if (ok && pc == 0u)
-      ok = wait_until([&] { return ld_relaxed<GPU>(global) == 0u && atom_cas_acquire<GPU>(global, 0u, 1u) == 0u; },
-                      [] {}, env, HS_SITE_SPIN_LOCK);
-  }
-  return __syncthreads_or(ok) != 0;
-}
-__device__ __forceinline__ void cohort_tas_unlock(unsigned* local, unsigned* global, unsigned pc, unsigned others) {
-  __syncthreads();  // every thread's critical-section stores precede the release
-  if (is_master()) {
-    if (others != 0u && pc + 1u < kCohortMaxPass) {
-      red_release_add<GPU>(local, 1u);
-    } else {
-      st_release<GPU>(global, 0u);
-      red_release_add<GPU>(local, 0u - (2u * pc + 1u));
-    }
-  }
-}
 
 // Ticket cohort: a ticket lock per die over the global ticket lock.  The local
 // turn word carries the pass count: turn = (ticket << 6) | passes, written
@@ -353,6 +312,44 @@ __device__ __forceinline__ void cohort_ticket_unlock(unsigned* lu, unsigned* gu,
       st_release<GPU>(lu, (next << 6) | (pc + 1u));  // pass the global lock on within the die
     } else {
       red_release_inc<GPU>(gu, wrap);
+      st_release<GPU>(lu, next << 6);
+    }
+  }
+}
+
+// Ticket cohort over any global lock (the spin, EBO and ring mutexes).  The
+// local layer is cohort_ticket_lock's (turn = (ticket << 6) | passes, written
+// only by the holder).  A TB whose turn comes without a pass runs `acquire`
+// (master thread; false on timeout) to take the global lock; the releasing
+// holder passes both locks to the next ticket of its die (at most
+// kCohortMaxPass times in a row) or runs `release` and advances the turn.
+// Only one TB per die touches the global lock word, and a pass is one release
+// store to a line homed on the die, with no atomic at all.
+template <class Acquire>
+__device__ __forceinline__ bool cohort_queue_lock(unsigned* lt, unsigned* lu, Acquire acquire, const HsEnv& env,
+                                                  unsigned site, unsigned& my, unsigned& pc, unsigned& snap) {
+  int ok = 0;
+  if (is_master()) {
+    my = atom_inc_relaxed<GPU>(lt, kCohortTicketWrap);
+    unsigned cur = 0;
+    ok = wait_until_p([&] { cur = ld_acquire<GPU>(lu); return (cur >> 6) == my; }, [&] { return cur; }, [] {}, env,
+                      site);
+    pc = cur & 63u;
+    snap = ld_relaxed<GPU>(lt);  // tickets taken so far; needed only at release
+    if (ok && pc == 0u) ok = acquire();
+  }
+  return __syncthreads_or(ok) != 0;
+}
+template <class Release>
+__device__ __forceinline__ void cohort_queue_unlock(unsigned* lu, Release release, unsigned my, unsigned pc,
+                                                    unsigned snap) {
+  __syncthreads();  // every thread's critical-section stores precede the release
+  if (is_master()) {
+    const unsigned next = (my >= kCohortTicketWrap) ? 0u : my + 1u;
+    if (snap != next && pc + 1u < kCohortMaxPass) {
+      st_release<GPU>(lu, (next << 6) | (pc + 1u));  // pass the global lock on within the die
+    } else {
+      release();
       st_release<GPU>(lu, next << 6);
     }
   }

@@ -1,4 +1,4 @@
-"""GPU: the die-aware cohort global mutexes (spin, EBO, FA).  Final storage
+"""GPU: the die-aware cohort global mutexes (spin, EBO, ring "sleep", FA).  Final storage
 must be bit-exact against the golden's closed form with the cohort lock and
 with HS_RUN_NO_COHORT, in every data mode and at every sweep size, including
 repeats that keep the ticket state; the run must report which lock ran."""
@@ -17,7 +17,7 @@ def _check(hs, cfg, seed):
     return r
 
 
-@pytest.mark.parametrize("prim", ["spinMutex", "spinMutexEBO", "faMutex"])
+@pytest.mark.parametrize("prim", ["spinMutex", "spinMutexEBO", "sleepMutex", "faMutex"])
 @pytest.mark.parametrize("mult,L", [(1, 10), (2, 10), (4, 100), (1, 100)])
 @pytest.mark.parametrize("mode", ["inc", "ref"])
 def test_cohort_exact(hs, prim, mult, L, mode):
@@ -38,15 +38,20 @@ def test_cohort_runs_on_this_part(hs):
     assert one.cohort == 0  # a single TB needs no lock hand-off
 
 
-@pytest.mark.parametrize("prim", ["spinMutex", "faMutex", "spinMutexEBO"])
+@pytest.mark.parametrize("prim", ["spinMutex", "faMutex", "spinMutexEBO", "sleepMutex"])
 def test_cohort_slice_and_reference_threads(hs, prim):
     nsm = hs.device_info()["nsm"]
     _check(hs, hs.RunConfig(prim, 10, 8, 100, threads=256, repeats=1, mode="slice"), 3)
     _check(hs, hs.RunConfig(prim, 10, 2 * nsm, 30, threads=32, repeats=10, mode="ref"), 4)
 
 
-def test_cohort_ticket_state_kept_across_repeats(hs):
+@pytest.mark.parametrize("prim", ["faMutex", "sleepMutex", "spinMutex"])
+def test_cohort_ticket_state_kept_across_repeats(hs, prim):
+    # die tickets, turns, the ring and the slot that travels with the passes
+    # carry over from launch to launch
     nsm = hs.device_info()["nsm"]
-    cfg = hs.RunConfig("faMutex", 10, nsm, 25, threads=256, repeats=3, mode="inc", flags=hs.RUN_KEEP_STATE)
+    _check(hs, hs.RunConfig(prim, 10, nsm, 25, threads=256, repeats=1, mode="inc"), 4)  # initialises the state
+    cfg = hs.RunConfig(prim, 10, nsm, 25, threads=256, repeats=3, mode="inc", flags=hs.RUN_KEEP_STATE)
     for seed in (5, 6):
-        _check(hs, cfg, seed)
+        r = _check(hs, cfg, seed)
+        assert r.cohort == 1
