@@ -273,25 +273,31 @@ def l2_atomic_peak(hs):
 # the release (one hand-off), wins its atomic, runs the critical section and
 # releases; a queue lock (ticket, ring slot) takes its place ahead of time, so
 # no atomic sits on the chain.
-LOCK_CHAIN = {"spinMutex": "cas", "spinMutexEBO": "cas", "faMutex": "queue", "sleepMutex": "queue",
-              "spinSem1": "cas", "spinSem2": "cas", "spinSem10": "cas", "spinSem120": "cas",
-              "spinSemEBO1": "cas", "spinSemEBO2": "cas", "spinSemEBO10": "cas", "spinSemEBO120": "cas"}
+# the hand-off chain of each lock primitive as this build runs it on a two-die
+# part: every global mutex is a die ticket queue in front of the primitive's
+# lock (a pass is a release store, no atomic), a semaphore's writers pass the
+# same way while its readers enter by CAS
+LOCK_CHAIN = {"spinMutex": "queue", "spinMutexEBO": "queue", "faMutex": "queue", "sleepMutex": "queue",
+              "spinSem1": "sem", "spinSem2": "sem", "spinSem10": "sem", "spinSem120": "sem",
+              "spinSemEBO1": "sem", "spinSemEBO2": "sem", "spinSemEBO10": "sem", "spinSemEBO120": "sem"}
 
 
 def lock_floors(hs, prims):
     """The per-op latency floor of each serialised lock primitive at each
     numLdSt, from measurements on this GPU:
 
-        floor(L) = hand-off + 2 x L2 load + (CAS lock ? atomic : 0) + (t1(L) - t1(10))
+        floor(L) = hand-off + 2 x L2 load + (CAS entry ? atomic : 0) + (t1(L) - t1(10))
 
     The first three terms are the chain of one contended op at numLdSt 10: the
     next holder sees the release (the median one-way flag latency between two
-    SMs), wins its atomic (a queue lock took its ticket or slot ahead of time),
-    loads its critical section and waits for its stores before releasing (two
-    L2 round trips).  The last term is the extra critical-section time of a
-    larger numLdSt: t1(L) is the time per op of the same primitive run by ONE TB
-    (1000 uncontended rounds), so t1(L) - t1(10) is the data movement one SM
-    adds, which no hand-off hides."""
+    SMs), wins its atomic (an op that enters by CAS: a semaphore reader; a queue
+    took its ticket ahead of time), loads its critical section and waits for
+    its stores before releasing (two L2 round trips).  The last term is the
+    extra critical-section time of a larger numLdSt: t1(L) is the time per op of
+    the same primitive run by ONE TB (1000 uncontended rounds), so
+    t1(L) - t1(10) is the data movement one SM adds, which no hand-off hides.
+    A mutex's floor is a number; a semaphore's is {"writer": queue chain,
+    "reader": CAS chain}, weighted per cell by its ops (cell_floor)."""
     lat = hs.probe_latency(256)
     h, a, ld = lat["handoff_ns_median"], lat["atomic_rtt_ns"], lat["load_rtt_ns"]
     t1 = {}
@@ -312,32 +318,51 @@ def lock_floors(hs, prims):
     floors = {}
     for (name, L), v in t1.items():
         extra = max(0.0, v - t1[(name, LDST[0])]) * 1e3 if (name, LDST[0]) in t1 else 0.0
-        floors[(name, L)] = (base[LOCK_CHAIN[name]] + extra) * 1e-3
+        if LOCK_CHAIN[name] == "sem":
+            floors[(name, L)] = {"writer": (base["queue"] + extra) * 1e-3, "reader": (base["cas"] + extra) * 1e-3}
+        else:
+            floors[(name, L)] = (base[LOCK_CHAIN[name]] + extra) * 1e-3
     return floors, {"handoff_ns": {"median": h, "min": lat["handoff_ns_min"], "max": lat["handoff_ns_max"],
                                    "partners": lat["partners"]},
                     "atomic_rtt_ns": a, "load_rtt_ns": ld,
                     "floor_ns": {"cas_lock": base["cas"], "queue_lock": base["queue"]},
                     "uncontended_us_per_op": {"%s/%d" % k: round(v, 4) for k, v in t1.items()},
-                    "floor_us_per_op": {"%s/%d" % k: round(v, 4) for k, v in floors.items()},
-                    "model": "floor = hand-off + 2 x L2 load + (CAS lock: atomic) + t1(numLdSt) - t1(10); t1 = one "
-                             "TB's uncontended time per op"}
+                    "floor_us_per_op": {"%s/%d" % k: (round(v, 4) if not isinstance(v, dict) else
+                                                      {r: round(x, 4) for r, x in v.items()})
+                                        for k, v in floors.items()},
+                    "model": "floor = hand-off + 2 x L2 load + (CAS entry: atomic) + t1(numLdSt) - t1(10); t1 = one "
+                             "TB's uncontended time per op; mutexes and semaphore writers pass through die queues "
+                             "(no atomic), semaphore readers enter by CAS; a semaphore cell's floor weights the two "
+                             "by its writer and reader ops"}
 
 
-def latency_roofline(cells, floors, kernel_prims, traffic):
+def cell_floor(c, floors, nsm):
+    """The per-op floor of one cell: a mutex's floor, or a semaphore's writer
+    and reader floors weighted by the cell's ops (one writer TB of the
+    numTBs_perSM TBs of each logical SM, main.cu:554-555)."""
+    f = floors[(c["prim"], c["num_ldst"])]
+    if not isinstance(f, dict):
+        return f
+    k = -(-c["num_tbs"] // min(c["num_tbs"], nsm))
+    return (f["writer"] + (k - 1) * f["reader"]) / k
+
+
+def latency_roofline(cells, floors, kernel_prims, traffic, nsm=None, kernel="k_mutex"):
     """bound "latency": the dominant kernel's cells against their floors.
     achieved = its ops / its time; peak = the same ops at the floor per op."""
     sel = [c for c in cells.values() if c["prim"] in kernel_prims and (c["prim"], c["num_ldst"]) in floors]
+    fl = {id(c): cell_floor(c, floors, nsm) for c in sel}
     ops = sum(c["ops"] for c in sel)
     ms = sum(c["mean_ms"] for c in sel)
-    floor_ms = sum(c["ops"] * floors[(c["prim"], c["num_ldst"])] * 1e-3 for c in sel)
+    floor_ms = sum(c["ops"] * fl[id(c)] * 1e-3 for c in sel)
     achieved = ops / (ms * 1e-3)
     peak = ops / (floor_ms * 1e-3)
-    return {"bound": "latency", "kernel": "k_mutex", "achieved": achieved, "peak": peak, "unit": "sync ops/s",
+    return {"bound": "latency", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "sync ops/s",
             "frac": achieved / peak, "peak_source": "measured (hs_probe_latency hand-off + uncontended op)",
             "traffic": traffic, "traffic_source": TRAFFIC_SOURCE,
             "cells": {cell_key(c["prim"], c["num_tbs"], c["num_ldst"]):
-                      {"us_per_op": round(c["us_per_op"], 4), "floor_us": round(floors[(c["prim"], c["num_ldst"])], 4),
-                       "frac": round(floors[(c["prim"], c["num_ldst"])] / c["us_per_op"], 3)} for c in sel},
+                      {"us_per_op": round(c["us_per_op"], 4), "floor_us": round(fl[id(c)], 4),
+                       "frac": round(fl[id(c)] / c["us_per_op"], 3)} for c in sel},
             "formula": "frac = sum(ops * floor_us) / sum(ops * us_per_op) over the dominant kernel's cells"}
 
 
@@ -724,7 +749,7 @@ def main():
             by_kernel[kernel_of(c["prim"])] = by_kernel.get(kernel_of(c["prim"]), 0.0) + c["mean_ms"]
         mutexes = [p for p in HEAD_PRIMS if p in LOCK_CHAIN]
         floors, lat = lock_floors(hs, SWEEP_PRIMS)
-        roofline = latency_roofline(cells, floors, mutexes, DRAM_BYTES_PER_LAUNCH)
+        roofline = latency_roofline(cells, floors, mutexes, DRAM_BYTES_PER_LAUNCH, nsm=nsm)
         roofline["share_of_device_time"] = by_kernel.get("k_mutex", 0.0) / sum(by_kernel.values())
         out = {
             "metric": "sync ops/s", "value": value, "unit": "sync ops/s", "n_gpus": world,
@@ -768,8 +793,7 @@ def main():
             sk = {}
             for c in allc.values():
                 sk[kernel_of(c["prim"])] = sk.get(kernel_of(c["prim"]), 0.0) + c["mean_ms"]
-            sem_roof = latency_roofline(scells, floors, SEM_PRIMS, None)
-            sem_roof["kernel"] = "k_sem"
+            sem_roof = latency_roofline(scells, floors, SEM_PRIMS, None, nsm=nsm, kernel="k_sem")
             sem_roof["traffic_source"] = None
             out["full_sweep"] = {
                 "workload": "16 SyncPrims (the headline 8 plus spinSem{1,2,10,120}, spinSemEBO{1,2,10,120}) x the "

@@ -1,6 +1,6 @@
 """bench.py's latency roofline, from stand-ins for the probe and the runs (no
-GPU): a lock's floor per op is one hand-off, two L2 loads and (for a CAS lock)
-one atomic, plus the extra time one uncontended TB spends on a larger numLdSt
+GPU): a lock's floor per op is one hand-off, two L2 loads and (for an op that
+enters by CAS) one atomic, plus the extra time one uncontended TB spends on a larger numLdSt
 than 10; the roofline fraction
 is the floor-weighted ops over the measured time of the dominant kernel's
 cells.  Also the sweep aggregate: each cell counts once at its mean time."""
@@ -44,14 +44,27 @@ class _HS:
 
 
 def test_floors():
-    floors, lat = bench.lock_floors(_HS, ["spinMutex", "faMutex", "lfTreeBarrUniq"])
-    assert set(floors) == {("spinMutex", 10), ("spinMutex", 100), ("faMutex", 10), ("faMutex", 100)}
-    assert abs(floors[("spinMutex", 10)] - (0.7 + 0.3 + 0.3)) < 1e-9
-    assert abs(floors[("spinMutex", 100)] - (0.7 + 0.3 + 0.3 + 2.0)) < 1e-9
+    floors, lat = bench.lock_floors(_HS, ["spinMutex", "faMutex", "spinSem1", "lfTreeBarrUniq"])
+    assert set(floors) == {(p, L) for p in ("spinMutex", "faMutex", "spinSem1") for L in (10, 100)}
+    # every mutex passes through a die queue: hand-off + 2 loads, no atomic
+    assert abs(floors[("spinMutex", 10)] - (0.7 + 0.3)) < 1e-9
+    assert abs(floors[("spinMutex", 100)] - (0.7 + 0.3 + 2.0)) < 1e-9
     assert abs(floors[("faMutex", 10)] - (0.7 + 0.3)) < 1e-9
     assert abs(floors[("faMutex", 100)] - (0.7 + 0.3 + 2.0)) < 1e-9
+    # a semaphore's writers pass through the die queue, its readers enter by CAS
+    w, r = floors[("spinSem1", 100)]["writer"], floors[("spinSem1", 100)]["reader"]
+    assert abs(w - (0.7 + 0.3 + 2.0)) < 1e-9 and abs(r - (0.7 + 0.3 + 0.3 + 2.0)) < 1e-9
     assert lat["floor_ns"] == {"cas_lock": 1300.0, "queue_lock": 1000.0}
     assert lat["handoff_ns"] == {"median": 700.0, "min": 400.0, "max": 800.0, "partners": 151}
+
+
+def test_semaphore_cell_floor_weights_writers_and_readers():
+    floors = {("spinSem2", 10): {"writer": 1.0, "reader": 1.4}}
+    cell = {"prim": "spinSem2", "num_ldst": 10}
+    # numTBs <= NUM_SM: every TB a writer; 2 per SM: half; 4 per SM: one in four
+    assert bench.cell_floor(dict(cell, num_tbs=100), floors, 152) == 1.0
+    assert abs(bench.cell_floor(dict(cell, num_tbs=304), floors, 152) - 1.2) < 1e-9
+    assert abs(bench.cell_floor(dict(cell, num_tbs=608), floors, 152) - 1.3) < 1e-9
 
 
 def _rec(prim, tbs, L, us_per_op, ops=1000):
@@ -76,5 +89,6 @@ def test_aggregate_and_roofline():
 def test_every_lock_primitive_has_a_chain():
     locks = [p for p in bench.SWEEP_PRIMS if "Barr" not in p]
     assert sorted(locks) == sorted(bench.LOCK_CHAIN)
-    assert {bench.LOCK_CHAIN[p] for p in ("faMutex", "sleepMutex")} == {"queue"}
+    assert {bench.LOCK_CHAIN[p] for p in bench.HEAD_PRIMS if "Barr" not in p} == {"queue"}
+    assert {bench.LOCK_CHAIN[p] for p in bench.SEM_PRIMS} == {"sem"}
     assert bench.HEAD_PRIMS == [p for p in bench.SWEEP_PRIMS if "Sem" not in p]
