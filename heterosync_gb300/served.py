@@ -93,8 +93,9 @@ def served_sweep(seed: int = 20260101, n: int = 256, iter_div: int = 50, slots: 
 
     * burst: every request published at once (the drain rate of a full queue);
     * peak: the highest offered Poisson rate whose window throughput stays within
-      `keep_up` of the offered rate, searched with the same open-loop driver
-      (from the burst rate down by halves, then bisection);
+      `keep_up` of the arrivals on two independent arrival sequences, searched
+      with the same open-loop driver (from the burst rate down by halves, then
+      bisection);
     * loads: Poisson arrivals at each fraction of that peak: offered and achieved
       rates, p50/p99 latency, and slowdown -- each request's latency over its
       latency when served alone -- at p50/p99 overall and p99 per request class.
@@ -137,11 +138,18 @@ def served_sweep(seed: int = 20260101, n: int = 256, iter_div: int = 50, slots: 
         hi, lo = burst, None
         rate = burst
         for tag in range(12):
-            ok, arr, lat, _ = run(rate, 100 + tag)
-            exact &= ok
-            arrived, completed = window_rates(arr, lat)
-            tried.append({"offered": rate, "window_arrived": arrived, "window_completed": completed})
-            if completed >= keep_up * arrived:
+            # a 256-request run is short beside its longest requests, so one
+            # arrival sequence can keep up by luck: a rate must keep up on two
+            keeps = True
+            for rep in range(2):
+                ok, arr, lat, _ = run(rate, 100 + 2 * tag + rep)
+                exact &= ok
+                arrived, completed = window_rates(arr, lat)
+                tried.append({"offered": rate, "window_arrived": arrived, "window_completed": completed})
+                keeps = completed >= keep_up * arrived
+                if not keeps:
+                    break
+            if keeps:
                 lo = rate
                 if rate >= hi:
                     break
@@ -149,8 +157,7 @@ def served_sweep(seed: int = 20260101, n: int = 256, iter_div: int = 50, slots: 
                 hi = rate
             if lo is None:
                 rate = rate / 2.0
-            elif len([t for t in tried if t["window_completed"] >= keep_up * t["window_arrived"]]) > search_steps or \
-                    hi - lo < 0.02 * lo:
+            elif tag + 1 > search_steps or hi - lo < 0.02 * lo:
                 break
             else:
                 rate = 0.5 * (lo + hi)
@@ -158,7 +165,8 @@ def served_sweep(seed: int = 20260101, n: int = 256, iter_div: int = 50, slots: 
         res["peak"] = {"requests_per_s": peak, "sync_ops_per_s": ops / (n / peak), "keep_up": keep_up,
                        "search": tried,
                        "definition": "highest offered Poisson rate at which the completions inside the middle 80%% "
-                                     "of the arrival window keep up with the arrivals there within %.0f%%"
+                                     "of the arrival window keep up with the arrivals there within %.0f%%, on "
+                                     "two arrival sequences"
                                      % ((1 - keep_up) * 100)}
         for i, f in enumerate(loads):
             ok, arr, lat, wall = run(f * peak, i)
