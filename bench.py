@@ -258,6 +258,19 @@ def cpu_baseline(nsm, prims=None, budget_s=15.0):
                       % (len(cells), min(iters_used), max(iters_used), budget_s)}
 
 
+L2_PROBE_BYTES = 48 << 20  # two 24 MiB buffers: well inside the 129 MB L2 (half of it per die)
+
+
+def l2_bandwidth_peak(hs):
+    """The L2-resident copy rate (hs_probe_l2_bandwidth), GB/s read + written."""
+    import ctypes
+    v = ctypes.c_double()
+    hs.lib().hs_probe_l2_bandwidth.argtypes = [ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p]
+    if hs.lib().hs_probe_l2_bandwidth(L2_PROBE_BYTES, 20, ctypes.byref(v)):
+        return None
+    return v.value
+
+
 def l2_atomic_peak(hs):
     import ctypes
     v = ctypes.c_double()
@@ -269,11 +282,7 @@ def l2_atomic_peak(hs):
     return v.value, same.value
 
 
-# How a lock op's chain runs under contention.  A CAS lock's next holder sees
-# the release (one hand-off), wins its atomic, runs the critical section and
-# releases; a queue lock (ticket, ring slot) takes its place ahead of time, so
-# no atomic sits on the chain.
-# the hand-off chain of each lock primitive as this build runs it on a two-die
+# The hand-off chain of each lock primitive as this build runs it on a two-die
 # part: every global mutex is a die ticket queue in front of the primitive's
 # lock (a pass is a release store, no atomic), a semaphore's writers pass the
 # same way while its readers enter by CAS
@@ -394,15 +403,28 @@ def cs_bytes(name, G, L, nsm, iters=ITERS):
 
 
 def secondary_bounds(hs, cells, nsm, dev_s):
-    """The HBM and L2-atomic fractions of the same cells (both tiny by
-    construction: a serialised lock uses neither bandwidth nor atomic rate)."""
+    """The HBM, L2-bandwidth and L2-atomic fractions of the same cells (tiny for
+    the serialised locks, which use neither bandwidth nor atomic rate), and the
+    L2-bandwidth fraction of each tree-barrier cell at numLdSt 100, whose
+    episodes move every TB's chunk through L2."""
     peak_gbs, peak_kind = load_peaks()
     byts = sum(cs_bytes(c["prim"], c["num_tbs"], c["num_ldst"], nsm) for c in cells.values())
     atom_peak, same_rate = l2_atomic_peak(hs)
+    l2_gbs = l2_bandwidth_peak(hs)
     atom = sum(c["ops"] * ATOMICS_PER_OP[c["prim"]] for c in cells.values()) / dev_s
+    barr = {}
+    for k, c in cells.items():
+        if "Barr" in c["prim"] and c["num_ldst"] == LDST[-1]:
+            gbs = cs_bytes(c["prim"], c["num_tbs"], c["num_ldst"], nsm) / (c["mean_ms"] * 1e-3) / 1e9
+            barr[k] = {"gbs": round(gbs, 1), "frac": round(gbs / l2_gbs, 3) if l2_gbs else None}
     return {"hbm": {"achieved": byts / dev_s / 1e9, "peak": peak_gbs, "unit": "GB/s",
                     "frac": byts / dev_s / 1e9 / peak_gbs, "peak_source": peak_kind,
                     "note": "critical-section bytes (L2-resident)"},
+            "l2_bandwidth": {"achieved": byts / dev_s / 1e9, "peak": l2_gbs, "unit": "GB/s",
+                             "frac": (byts / dev_s / 1e9 / l2_gbs) if l2_gbs else None,
+                             "peak_source": "measured (hs_probe_l2_bandwidth: L2-resident copy, %d MiB, L1 bypassed)"
+                                            % (L2_PROBE_BYTES >> 20),
+                             "barrier_cells_numldst_%d" % LDST[-1]: barr},
             "l2_atomic": {"achieved": atom, "peak": atom_peak, "frac": (atom / atom_peak) if atom_peak else None,
                           "unit": "atomics/s", "same_address_rate": same_rate,
                           "note": "peak: contention-free red.add probe; same_address_rate: one word"}}
@@ -453,9 +475,15 @@ def exchange_extra(hs):
             rows["%s_cluster%d" % ("lf" if lf else "atomic", cl)] = {
                 "episodes_per_s": round(r.episodes_per_s), "exchange_gbs": round(r.exchange_gbs, 1),
                 "ms": round(r.elapsed_ms, 3)}
+    l2_gbs = l2_bandwidth_peak(hs)
+    best = max(rows.values(), key=lambda r: r["exchange_gbs"])
     return {"workload": "592 CTAs x 256 threads, fp32[4096] per CTA rotated to CTA b+1 each episode, "
                         "1000 episodes, one tree barrier per episode (bit-exact rotation checked)",
-            "exchange_bytes_per_episode": 592 * 4096 * 4 * 2, "results": rows}
+            "exchange_bytes_per_episode": 592 * 4096 * 4 * 2, "results": rows,
+            "l2_bandwidth": {"peak_gbs": l2_gbs, "best_exchange_gbs": best["exchange_gbs"],
+                             "frac": round(best["exchange_gbs"] / l2_gbs, 3) if l2_gbs else None,
+                             "note": "most of the exchange moves SM to SM through distributed shared memory, so "
+                                     "the L2 copy rate is a reference point, not its bound"}}
 
 
 def batch_extra(hs):

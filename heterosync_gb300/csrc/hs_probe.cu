@@ -9,6 +9,11 @@
 // word, words 128 bytes apart, so no two atomics contend for a line: the
 // aggregate rate is the chip's contention-free L2 atomic throughput, the
 // denominator of the sync-ops roofline.
+//
+// L2 bandwidth: a copy between two buffers that together fit in L2, with
+// loads and stores that bypass L1 (ld/st .cg), repeated in one launch: the
+// chip's L2-resident copy rate, the denominator for critical sections and
+// exchanges whose data stays in L2.
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cstdint>
@@ -32,6 +37,24 @@ __global__ void __launch_bounds__(1024) k_probe_red(unsigned* words, int iters, 
 __global__ void k_probe_same(unsigned* word, int iters) {
   if (threadIdx.x == 0)
     for (int i = 0; i < iters; ++i) asm volatile("red.relaxed.gpu.global.add.u32 [%0], 1;" :: "l"(word) : "memory");
+}
+
+// L2-resident copy: grid-stride, four 16-byte loads in flight per thread, L1 bypassed.
+__global__ void __launch_bounds__(512) k_probe_copy(const uint4* __restrict__ src, uint4* __restrict__ dst,
+                                                    size_t n, int reps) {
+  const size_t step = (size_t)gridDim.x * blockDim.x;
+  for (int r = 0; r < reps; ++r) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * step < n; i += 4 * step) {
+      const uint4 a = __ldcg(src + i), b = __ldcg(src + i + step), c = __ldcg(src + i + 2 * step),
+                  d = __ldcg(src + i + 3 * step);
+      __stcg(dst + i, a);
+      __stcg(dst + i + step, b);
+      __stcg(dst + i + 2 * step, c);
+      __stcg(dst + i + 3 * step, d);
+    }
+    for (; i < n; i += step) __stcg(dst + i, __ldcg(src + i));
+  }
 }
 
 constexpr unsigned long long kLatTimeoutNs = 2000000000ull;
@@ -187,5 +210,43 @@ extern "C" int hs_probe_l2_atomics(int blocks, int threads, int iters, int same_
   if (e != cudaSuccess) return HS_ECUDA;
   const double total = same_address ? (double)blocks * iters : (double)blocks * threads * iters;
   *atomics_per_s = total / (ms * 1e-3);
+  return HS_OK;
+}
+
+extern "C" int hs_probe_l2_bandwidth(size_t bytes, int reps, double* copy_gbs) {
+  if (bytes < (1u << 20) || reps <= 0 || reps > 10000 || !copy_gbs) return HS_EINVAL;
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) {
+    cudaGetLastError();
+    return HS_ENODEV;
+  }
+  const size_t n = bytes / 2 / sizeof(uint4);  // vectors per buffer
+  uint4 *src = nullptr, *dst = nullptr;
+  if (cudaMalloc(&src, n * sizeof(uint4)) != cudaSuccess || cudaMalloc(&dst, n * sizeof(uint4)) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(src);
+    return HS_ENORES;
+  }
+  cudaMemset(src, 1, n * sizeof(uint4));
+  cudaMemset(dst, 0, n * sizeof(uint4));
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  const unsigned grid = (unsigned)nsm * 4u;
+  hs::k_probe_copy<<<grid, 512>>>(src, dst, n, 2);  // warm-up: both buffers into L2
+  cudaEventRecord(a);
+  hs::k_probe_copy<<<grid, 512>>>(src, dst, n, reps);
+  cudaEventRecord(b);
+  cudaError_t e = cudaEventSynchronize(b);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  hs_note_launches(2);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(src);
+  cudaFree(dst);
+  if (e != cudaSuccess) return HS_ECUDA;
+  *copy_gbs = 2.0 * (double)n * sizeof(uint4) * reps / (ms * 1e-3) * 1e-9;  // bytes read + written
   return HS_OK;
 }

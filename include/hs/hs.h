@@ -390,6 +390,12 @@ int hs_serve_drive(hs_server* s, const hs_serve_request* reqs, int n, const uint
  * contended lock word sustains).  Result in atomics per second. */
 int hs_probe_l2_atomics(int blocks, int threads, int iters, int same_address, double* atomics_per_s);
 
+/* L2-resident copy bandwidth: two buffers of bytes/2 each (together well under
+ * the L2's size), copied `reps` times in one launch with loads and stores that
+ * bypass L1, after one warm-up launch.  Result: bytes read + written per second,
+ * in GB/s. */
+int hs_probe_l2_bandwidth(size_t bytes, int reps, double* copy_gbs);
+
 /* The latencies a lock hand-off is made of, each measured by one thread:
  *  handoff: CTA 0 and each other CTA (one per SM, cooperative launch) ping-pong
  *           a flag `rounds` times (st.release.gpu, then ld.acquire.gpu polls until

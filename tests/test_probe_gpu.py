@@ -1,5 +1,6 @@
-"""GPU: the roofline probes.  The L2 atomic rate and the lock hand-off
-latencies must come back finite, ordered and in physically sensible ranges."""
+"""GPU: the roofline probes.  The L2 atomic rate, the L2-resident copy rate and
+the lock hand-off latencies must come back finite, ordered and in physically
+sensible ranges."""
 import ctypes
 
 import pytest
@@ -27,3 +28,13 @@ def test_latency_probe(hs):
 def test_latency_probe_rejects_bad_rounds(hs):
     r = ctypes.c_char * 64
     assert hs.lib().hs_probe_latency(0, ctypes.byref(r())) == hs.HS_EINVAL
+
+
+def test_l2_bandwidth_probe(hs):
+    lib = hs.lib()
+    lib.hs_probe_l2_bandwidth.argtypes = [ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p]
+    v = ctypes.c_double()
+    assert lib.hs_probe_l2_bandwidth(48 << 20, 10, ctypes.byref(v)) == 0
+    assert 100.0 < v.value < 100000.0  # GB/s
+    assert lib.hs_probe_l2_bandwidth(1024, 10, ctypes.byref(v)) == hs.HS_EINVAL
+    assert lib.hs_probe_l2_bandwidth(48 << 20, 0, ctypes.byref(v)) == hs.HS_EINVAL
