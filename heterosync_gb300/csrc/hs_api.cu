@@ -19,6 +19,7 @@ cudaError_t prepare_smem(KernelFn fn, size_t smem_bytes);
 size_t barrier_tile_bytes(int threads, int num_ldst, int num_tbs, int phys_nsm, size_t base);
 KernelFn prim_cluster_kernel(int mode);
 KernelFn barrier_group_kernel(int prim, int mode);
+KernelFn barrier_group_tma_kernel(int prim, int mode);
 cudaError_t launch_ring_init(unsigned* ring, unsigned slots_per_group, unsigned groups, cudaStream_t st);
 cudaError_t launch_fill_lines(unsigned* base, size_t n, size_t stride, unsigned value, cudaStream_t st);
 }  // namespace hs
@@ -599,6 +600,36 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c0, void* storage, int o
     }
     cudaGetLastError();
   }
+  // Above numLdSt 64 the same group CTA gives each member its own bulk-copy
+  // buffer (k_barrier_grp_tma): the members' copies stay in flight side by side,
+  // as with one CTA per TB, while the local stage stays the CTA barrier.
+  // Measured at numLdSt 100 (us per episode): lfTreeBarrUniq at 304 TBs 7.12
+  // against 8.68 with one CTA per TB, at 608 TBs 11.54 against 12.83.
+  unsigned tile_cap = 0;
+  if (is_barrier(c->prim) && c->mode != HS_MODE_SLICE && c->num_ldst > 64 &&
+      !(c->flags & (HS_RUN_NO_CLUSTER | HS_RUN_NO_GROUP_CTA | HS_RUN_REGISTER_CS)) && c->skip_tb < 0 &&
+      variant != PV_NAIVE && variant != PV_NAIVE_ALL && tbs_per_cta == 1 && c->threads % 32 == 0) {
+    const int nb = c->num_tbs < nsm ? c->num_tbs : nsm;
+    const int m = c->num_tbs / nb;
+    KernelFn gfn = barrier_group_tma_kernel(c->prim, c->mode);
+    const size_t region = (size_t)64 * (c->num_ldst + 1);
+    const size_t chunk = region * (size_t)(c->threads / 16);
+    const size_t cap = m >= 1 ? std::min(chunk, (size_t)(216 * 1024) / (size_t)m / region * region) : 0;
+    int per_sm = 0;
+    if (gfn && m >= 2 && m <= 15 && c->num_tbs % nb == 0 && m * c->threads <= 1024 &&
+        m * c->threads <= ctx->max_tpb && cap >= region &&
+        cudaFuncSetAttribute((const void*)gfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(m * cap)) ==
+            cudaSuccess &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gfn, m * c->threads, m * cap) == cudaSuccess &&
+        (long long)per_sm * ctx->nsm >= nb) {
+      fn = gfn;
+      smem = m * cap;
+      tile_cap = (unsigned)cap;
+      block = m * c->threads;
+      tbs_per_cta = m;
+    }
+    cudaGetLastError();
+  }
   if (is_barrier(c->prim) && tbs_per_cta == 1) {
     const int nb = c->num_tbs < nsm ? c->num_tbs : nsm;
     const int m = c->num_tbs / nb;
@@ -689,6 +720,7 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c0, void* storage, int o
   d.cluster = cluster;
   d.variant = variant;
   d.grp = tbs_per_cta;
+  d.tile_cap = tile_cap;
   r->cluster = cluster;
   r->tbs_per_cta = tbs_per_cta;
   // global mutex, or global semaphore (its writers), with more than one TB:

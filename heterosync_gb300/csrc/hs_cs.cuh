@@ -415,6 +415,78 @@ __device__ __forceinline__ bool cs_read_tma(const RunDesc& d, int chunk, TmaCtx&
   return true;
 }
 
+// Tiled bulk-copy critical section run by ONE sub-block of a CTA that hosts a
+// whole logical-SM group (the group-CTA tree barrier at numLdSt > 64): the T
+// threads [r*T, (r+1)*T) work on their own chunk through their own buffer and
+// mbarrier, thread tid 0 issuing the copies, and synchronise on named barrier
+// `bar` (1..15) instead of the CTA barrier.  Each member thus keeps its own
+// load and stores in flight, as one-CTA-per-TB launches do: one CTA moving all
+// the group's chunks through shared buffers ran at half their speed.
+__device__ __forceinline__ void sub_sync(int bar, int T) {
+  asm volatile("bar.sync %0, %1;" :: "r"(bar), "r"(T) : "memory");
+}
+__device__ __forceinline__ bool sub_and(int bar, int T, int v) {
+  int r;
+  asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.s32 p, %1, 0;\n\tbar.red.and.pred q, %2, %3, p;\n\t"
+               "selp.s32 %0, 1, 0, q;\n\t}"
+               : "=r"(r) : "r"(v), "r"(bar), "r"(T) : "memory");
+  return r != 0;
+}
+
+template <int MODE>
+__device__ __forceinline__ bool cs_chunk_tma_sub(const RunDesc& d, int chunk, TmaCtx& t, unsigned buf_bytes,
+                                                 const HsEnv& env, int bar, int tid) {
+  unsigned char* c = reinterpret_cast<unsigned char*>(d.data + (size_t)chunk * chunk_words(d.T, d.L));
+  const int T = d.T, R = T >> 4;
+  const unsigned rb = (unsigned)(64 * (d.L + 1));
+  int per = (int)(buf_bytes / rb);
+  if (per < 1) per = 1;
+  const unsigned sbase = smem_addr(t.buf);
+  for (int r0 = 0; r0 < R; r0 += per) {
+    const int n = (R - r0 < per) ? (R - r0) : per;
+    unsigned char* src = c + (size_t)r0 * rb;
+    int ok = 1;
+    if (tid == 0) {
+      asm volatile("fence.proxy.async.global;" ::: "memory");
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(t.mbar), "r"((unsigned)n * rb)
+                   : "memory");
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                   :: "r"(sbase), "l"(src), "r"((unsigned)n * rb), "r"(t.mbar) : "memory");
+      ok = tma_wait(t, env);
+    }
+    t.phase ^= 1u;
+    if (!sub_and(bar, T, ok)) return false;
+    unsigned first = 0u;
+    if constexpr (MODE == M_INC) {
+      const int per_region = d.L * 4, rw4 = (d.L + 1) * 4;
+      uint4* s4 = reinterpret_cast<uint4*>(t.buf);
+      for (int i = tid; i < n * per_region; i += T) {
+        const int h = i / per_region;
+        uint4& v = s4[h * rw4 + 4 + (i - h * per_region)];
+        v.x += 1u; v.y += 1u; v.z += 1u; v.w += 1u;
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      sub_sync(bar, T);
+      first = 1u;
+    }
+    if (tid == 0) {
+      for (int h = 0; h < n; ++h) {
+        asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                     :: "l"(src + (size_t)h * rb + 64u), "r"(sbase + h * rb + first * 64u), "r"((unsigned)(64 * d.L))
+                     : "memory");
+      }
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+      asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // buffer free for the next tile
+    }
+    sub_sync(bar, T);
+  }
+  if (tid == 0) {
+    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");  // writes complete before the release
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+  }
+  return true;
+}
+
 // Vector depth V = 16-byte vectors each thread keeps in flight per pass.  The
 // launch bound follows from it: V 4 -> 1024 threads, 8 -> 512, 26 -> 256 (a
 // 256-thread TB then moves numLdSt <= 104 lines of its chunk in one pass).

@@ -44,6 +44,7 @@ struct RunDesc {
   int skip_tb;          // logical TB that never arrives at a barrier (-1: none)
   int cluster;          // CTAs per cluster for barrier kernels (1: no clusters)
   int grp;              // tree barriers: logical TBs one CTA hosts (0 or 1: one CTA per TB)
+  unsigned tile_cap;    // group-CTA bulk-copy barrier: bytes per staging buffer
   // line offsets inside `locks`
   int l_glob;           // global barrier: +0 count, +1 gen, +2 go
   int l_gflag;          // global barrier flags (dense, one word per group)

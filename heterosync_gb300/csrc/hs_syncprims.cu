@@ -547,6 +547,56 @@ __global__ void __launch_bounds__(1024, 1) k_barrier_grp(RunDesc d) {
   }
 }
 
+// The group-CTA tree barrier with bulk-copy critical sections (numLdSt > 64,
+// where the register path of k_barrier_grp loses to bulk copies).  Member r
+// (threads [r*T, (r+1)*T)) works on its chunks exactly as in k_barrier_grp,
+// through its own d.tile_cap-byte buffer and mbarrier, synchronising on named
+// barrier r + 1 inside its critical section; the local stage is still the CTA
+// barrier.  At most 15 members (named barriers 1..15), T a multiple of 32.
+template <bool LF, bool EXCH, int MODE>
+__global__ void __launch_bounds__(1024, 1) k_barrier_grp_tma(RunDesc d) {
+  __shared__ unsigned long long s_mbar[15];
+  extern __shared__ __align__(128) unsigned char dyn_smem[];
+  const int T = d.T;
+  const int nb = (int)gridDim.x;
+  const int Gd = d.num_tbs;
+  const int g = (int)blockIdx.x;
+  const int r = (int)threadIdx.x / T;
+  const int tid = (int)threadIdx.x - r * T;
+  const HsEnv env{d.status, d.timeout_ns};
+  TmaCtx tma;
+  tma.buf = dyn_smem + (size_t)r * d.tile_cap;
+  tma.mbar = smem_addr(s_mbar + r);
+  tma.phase = 0u;
+  tma.cap = d.tile_cap;
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(tma.mbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __shared__ BarState s_init;
+  if (is_master()) {
+    s_init.lgen = 0u;
+    s_init.ggen = LF ? ld_relaxed<GPU>(d.locks + (size_t)(d.l_glob + 2) * kLineWords)
+                     : ld_relaxed<GPU>(d.locks + (size_t)(d.l_glob + 1) * kLineWords);
+  }
+  __syncthreads();
+  BarState s = s_init;
+  const int phases = EXCH ? 2 : 1;
+  int cur = g + r * nb;
+  for (int i = 0; i < d.iters; ++i) {
+    for (int ph = 0; ph < phases; ++ph) {
+      if (ph == 1) cur = (cur + nb) % Gd;
+      const bool ok = cs_chunk_tma_sub<MODE>(d, cur, tma, d.tile_cap, env, r + 1, tid);
+      // every member reaches this CTA barrier (a member whose copy wait gave up
+      // returned from its critical section whole); between the phases it is
+      // also the local barrier: every member's stores are complete
+      if (__syncthreads_or(!ok)) return;
+    }
+    if (!tree_barrier<LF>(d, g, 0, 1, nb, s, env)) return;
+    cur = (cur + 1) % Gd;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Ring initialisation: slot 0 of every group's ring = 1, the rest = -1
 // (cudaLocks.cu:58-65).
@@ -579,6 +629,30 @@ KernelFn barrier_group_kernel(int prim, int mode) {
       case P_ATOMIC_TREE_EXCH: return k_barrier_grp<false, true, M_INC, 8>;
       case P_LF_TREE: return k_barrier_grp<true, false, M_INC, 8>;
       case P_LF_TREE_EXCH: return k_barrier_grp<true, true, M_INC, 8>;
+      default: return nullptr;
+    }
+  }
+  return nullptr;
+}
+
+// The same with bulk-copy critical sections (two staging buffers of
+// d.tile_cap bytes in dynamic shared memory).
+KernelFn barrier_group_tma_kernel(int prim, int mode) {
+  if (mode == M_REF) {
+    switch (prim) {
+      case P_ATOMIC_TREE: return k_barrier_grp_tma<false, false, M_REF>;
+      case P_ATOMIC_TREE_EXCH: return k_barrier_grp_tma<false, true, M_REF>;
+      case P_LF_TREE: return k_barrier_grp_tma<true, false, M_REF>;
+      case P_LF_TREE_EXCH: return k_barrier_grp_tma<true, true, M_REF>;
+      default: return nullptr;
+    }
+  }
+  if (mode == M_INC) {
+    switch (prim) {
+      case P_ATOMIC_TREE: return k_barrier_grp_tma<false, false, M_INC>;
+      case P_ATOMIC_TREE_EXCH: return k_barrier_grp_tma<false, true, M_INC>;
+      case P_LF_TREE: return k_barrier_grp_tma<true, false, M_INC>;
+      case P_LF_TREE_EXCH: return k_barrier_grp_tma<true, true, M_INC>;
       default: return nullptr;
     }
   }

@@ -57,8 +57,9 @@ enum {
                              logical TB, the critical section split over its SMs, for every such run (by
                              default only semaphores whose writers own 4 or more chunks, where it is faster) */
   HS_RUN_NO_GROUP_CTA = 128 /* tree barriers: one CTA per logical TB even where a whole logical-SM group
-                               fits one CTA (by default such a group, numLdSt <= 64, runs as one CTA of
-                               numTBs_perSM x threads, its local stage the CTA barrier) */
+                               fits one CTA (by default such a group runs as one CTA of numTBs_perSM x
+                               threads, its local stage the CTA barrier: register critical sections up
+                               to numLdSt 64, a bulk-copy buffer per member above) */
 };
 
 /* One run of one SyncPrims primitive: `repeats` launches of `num_tbs` TBs of

@@ -121,10 +121,10 @@ def test_uneven_barrier_groups_complete(hs, oracle):
 @pytest.mark.parametrize("L", [10, 64, 100])
 def test_barrier_groups_on_clusters(hs, oracle, prim, mult, L):
     """numTBs = mult * NUM_SM: each logical-SM group runs as one CTA of mult x
-    256 threads (numLdSt <= 64, register path: the local stage is the CTA
-    barrier), or as one thread-block cluster (local stage = hardware cluster
-    barrier), or flat; every form's result equals the golden's, on the register
-    path and the tiled bulk-copy path (numLdSt 64 and 100 without group CTAs)."""
+    256 threads (the local stage is the CTA barrier; register path up to
+    numLdSt 64, two bulk-copy buffers above), or as one thread-block cluster
+    (local stage = hardware cluster barrier), or flat; every form's result
+    equals the golden's, on the register path and the tiled bulk-copy path."""
     nsm = hs.device_info()["nsm"]
     G = mult * nsm
     outs = []
@@ -135,7 +135,7 @@ def test_barrier_groups_on_clusters(hs, oracle, prim, mult, L):
         st = init.copy()
         res = hs.run(cfg, st)
         assert res.status == 0
-        if flags == 0 and L <= 64:
+        if flags == 0:
             assert res.tbs_per_cta == mult and res.cluster == 1   # one CTA per logical-SM group
         else:
             assert res.tbs_per_cta == 1
@@ -168,6 +168,31 @@ def test_barrier_group_cta_shapes(hs, oracle, prim, T, mult, nsm, mode):
     res = hs.run(cfg, st)
     assert res.status == 0 and res.tbs_per_cta == mult
     assert np.array_equal(st, oracle.golden(prim, T, 9, mult * n, 5, 3, n, mode == "inc", init))
+
+
+@pytest.mark.parametrize("prim", [0, 1, 2, 3])
+@pytest.mark.parametrize("T,mult,nsm,L", [(256, 2, 0, 100), (256, 4, 7, 127), (128, 8, 6, 65), (64, 15, 5, 80),
+                                          (256, 3, 4, 100), (32, 8, 6, 70)])
+@pytest.mark.parametrize("mode", ["ref", "inc"])
+def test_barrier_group_cta_bulk_copies(hs, oracle, prim, T, mult, nsm, L, mode):
+    """The group-CTA form above numLdSt 64: the group's chunks go through two
+    bulk-copy buffers (tiles that split a chunk at numLdSt 127, many small
+    chunks at 64 threads), three launches; equal to the literal golden and to
+    the one-CTA-per-TB form."""
+    dev_nsm = hs.device_info()["nsm"]
+    n = nsm or dev_nsm
+    outs = []
+    for flags in (0, hs.RUN_NO_GROUP_CTA):
+        cfg = hs.RunConfig(prim=prim, num_ldst=L, num_tbs=mult * n, num_iters=4, threads=T, repeats=3, mode=mode,
+                           nsm=nsm, flags=flags, timeout_ns=5_000_000_000)
+        init = _init(hs.storage_words(cfg), 17 * prim + mult + L)
+        st = init.copy()
+        res = hs.run(cfg, st)
+        assert res.status == 0 and res.tbs_per_cta == (mult if flags == 0 else 1)
+        outs.append(st)
+    want = oracle.golden(prim, T, L, mult * n, 4, 3, n, mode == "inc", init)
+    for o in outs:
+        assert np.array_equal(o, want)
 
 
 @pytest.mark.parametrize("prim", [20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30, 31])
