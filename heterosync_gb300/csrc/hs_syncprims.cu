@@ -133,10 +133,10 @@ __device__ __forceinline__ void mutex_loop(const RunDesc& d, int g, int r, int m
 template <int KIND, bool UNIQ, int MODE, int V, bool TMA = false>
 __global__ void __launch_bounds__(TMA ? 256 : Bounds<V>::kThreads) k_mutex(RunDesc d) {
   __shared__ int s_slot;
-  __shared__ unsigned long long s_mbar;
+  __shared__ unsigned long long s_mbar[kTmaParts];
   extern __shared__ __align__(128) unsigned char dyn_smem[];
   TmaCtx tma;
-  if constexpr (TMA) tma_init(tma, &s_mbar, dyn_smem);
+  if constexpr (TMA) tma_init(tma, s_mbar, dyn_smem, kTmaParts);
   const unsigned wrap = UNIQ ? 100000000u : 1000000000u;  // cudaLocksMutexFA.cu:24,83
   const HsEnv env{d.status, d.timeout_ns};
   if constexpr (UNIQ) {
@@ -216,10 +216,10 @@ __device__ __forceinline__ void sem_loop(const RunDesc& d, int b, int numSM, int
 // ---------------------------------------------------------------------------
 template <bool EBO, bool UNIQ, int MODE, int V, bool TMA = false>
 __global__ void __launch_bounds__(TMA ? 256 : Bounds<V>::kThreads) k_sem(RunDesc d) {
-  __shared__ unsigned long long s_mbar;
+  __shared__ unsigned long long s_mbar[kTmaParts];
   extern __shared__ __align__(128) unsigned char dyn_smem[];
   TmaCtx tma;
-  if constexpr (TMA) tma_init(tma, &s_mbar, dyn_smem);
+  if constexpr (TMA) tma_init(tma, s_mbar, dyn_smem, kTmaParts);
   const HsEnv env{d.status, d.timeout_ns};
   const int Gd = d.num_tbs;
   const int numSM = Gd < d.nsm ? Gd : d.nsm;
