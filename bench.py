@@ -283,9 +283,10 @@ def l2_atomic_peak(hs):
 
 
 # The hand-off chain of each lock primitive as this build runs it on a two-die
-# part: every global mutex is a die ticket queue in front of the primitive's
-# lock (a pass is a release store, no atomic), a semaphore's writers pass the
-# same way while its readers enter by CAS
+# part: the spin, EBO and ticket mutexes are a die ticket queue in front of the
+# primitive's lock (a pass is a release store, no atomic), the ring mutex hands
+# its slot on (a queue lock), a semaphore's writers pass as the mutexes do while
+# its readers enter by CAS
 LOCK_CHAIN = {"spinMutex": "queue", "spinMutexEBO": "queue", "faMutex": "queue", "sleepMutex": "queue",
               "spinSem1": "sem", "spinSem2": "sem", "spinSem10": "sem", "spinSem120": "sem",
               "spinSemEBO1": "sem", "spinSemEBO2": "sem", "spinSemEBO10": "sem", "spinSemEBO120": "sem"}
@@ -341,8 +342,8 @@ def lock_floors(hs, prims):
                                         for k, v in floors.items()},
                     "model": "floor = hand-off + 2 x L2 load + (CAS entry: atomic) + t1(numLdSt) - t1(10); t1 = one "
                              "TB's uncontended time per op; mutexes and semaphore writers pass through die queues "
-                             "(no atomic), semaphore readers enter by CAS; a semaphore cell's floor weights the two "
-                             "by its writer and reader ops"}
+                             "or hand on a ring slot (no atomic), semaphore readers enter by CAS; a semaphore "
+                             "cell's floor weights the two by its writer and reader ops"}
 
 
 def cell_floor(c, floors, nsm):

@@ -723,9 +723,11 @@ extern "C" int hs_run(hs_ctx* ctx, const hs_run_config* c0, void* storage, int o
   d.tile_cap = tile_cap;
   r->cluster = cluster;
   r->tbs_per_cta = tbs_per_cta;
-  // global mutex, or global semaphore (its writers), with more than one TB:
-  // the die-aware cohort form
-  if (c->prim >= 4 && c->prim <= 15 && c->num_tbs > 1 && grid == c->num_tbs &&
+  // global spin, EBO and ticket mutexes, or global semaphore (its writers), with
+  // more than one TB: the die-aware cohort form.  The ring ("sleep") mutex is a
+  // queue lock already; in front of it a die queue measured no faster at
+  // numLdSt 10 and 3% slower at 100, so it stays plain.
+  if (c->prim >= 4 && c->prim <= 15 && c->prim != 6 && c->num_tbs > 1 && grid == c->num_tbs &&
       !(c->flags & HS_RUN_NO_COHORT) && cohort_ready(ctx)) {
     d.cohort = 1;
     d.die_map = reinterpret_cast<const unsigned char*>(ctx->coh_pool);

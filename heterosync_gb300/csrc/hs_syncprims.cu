@@ -33,31 +33,17 @@ template <int S, int KIND, int MODE, int V, bool TMA>
 __device__ __forceinline__ void mutex_loop(const RunDesc& d, int g, int r, int m, int G, unsigned* w0, unsigned* w1,
                                            unsigned* w2, unsigned* ring, unsigned ring_max, unsigned wrap,
                                            int* s_slot, TmaCtx& tma, const HsEnv& env) {
-  if constexpr (S == GPU) {
+  if constexpr (S == GPU && KIND != MK_SLEEP) {
     if (d.cohort) {  // global mutex as a cohort of per-die ticket queues (hs_device.cuh)
       unsigned sm;
       asm volatile("mov.u32 %0, %%smid;" : "=r"(sm));
       const int die = d.die_map[sm & 255u] & 1;
       unsigned* const* c = d.coh + 3 * die;
-      unsigned my = 0, pc = 0, aux = 0, slot = 0;  // meaningful in the master thread
+      unsigned my = 0, pc = 0, aux = 0;  // meaningful in the master thread
       for (int j = 0; j < d.iters; ++j) {
         bool ok;
         if constexpr (KIND == MK_FA) {
           ok = cohort_ticket_lock(c[0], c[1], w0, w1, wrap, d.bo_unit, d.bo_max, env, my, pc, aux);
-        } else if constexpr (KIND == MK_SLEEP) {
-          // the ring slot that holds the global lock travels with the passes (line 2)
-          ok = cohort_queue_lock(
-              c[0], c[1],
-              [&] {
-                slot = atom_inc_relaxed<GPU>(w2, ring_max);
-                unsigned* mine = ring + (size_t)slot * kRingStride;
-                unsigned* prev = ring + (size_t)(slot == 0u ? ring_max : slot - 1u) * kRingStride;
-                return wait_until_p([&] { return ld_acquire<GPU>(mine) == 1u; },
-                                    [&] { return ld_relaxed<GPU>(prev); }, [&] { sleep_ns(d.bo_unit); }, env,
-                                    HS_SITE_SLEEP_LOCK);
-              },
-              env, HS_SITE_SLEEP_LOCK, my, pc, aux);
-          if (is_master() && pc != 0u) slot = ld_relaxed<GPU>(c[2]);
         } else {
           ok = cohort_queue_lock(
               c[0], c[1],
@@ -81,16 +67,6 @@ __device__ __forceinline__ void mutex_loop(const RunDesc& d, int g, int r, int m
         else cs_chunk<MODE, V>(d, g);
         if constexpr (KIND == MK_FA) {
           cohort_ticket_unlock(c[1], w1, wrap, my, pc, aux);
-        } else if constexpr (KIND == MK_SLEEP) {
-          if (is_master()) st_relaxed<GPU>(c[2], slot);  // ordered before the pass by its release
-          cohort_queue_unlock(
-              c[1],
-              [&] {
-                const unsigned next = (slot >= ring_max) ? 0u : slot + 1u;
-                st_relaxed<GPU>(ring + (size_t)slot * kRingStride, 0xFFFFFFFFu);
-                st_release<GPU>(ring + (size_t)next * kRingStride, 1u);
-              },
-              my, pc, aux);
         } else {
           cohort_queue_unlock(c[1], [&] { st_release<GPU>(w0, 0u); }, my, pc, aux);
         }

@@ -50,9 +50,9 @@ enum {
   HS_RUN_REGISTER_CS = 8, /* critical sections on the register path only (no bulk copies through shared memory) */
   HS_RUN_GRAPH = 16,      /* the repeats as one CUDA graph: captured once per context and launch shape, then
                              replayed (not with HS_RUN_SYNC_EACH); the lock state is still reset before it */
-  HS_RUN_NO_COHORT = 32,  /* global mutexes and global semaphores' writers: the primitive's lock alone
-                             instead of the die-aware cohort (a ticket queue per die, homed on it, in front
-                             of the lock, which is handed on within the die) */
+  HS_RUN_NO_COHORT = 32,  /* global spin, EBO and ticket mutexes and global semaphores' writers: the
+                             primitive's lock alone instead of the die-aware cohort (a ticket queue per die,
+                             homed on it, in front of the lock, which is handed on within the die) */
   HS_RUN_CLUSTER_CS = 64, /* global mutexes and semaphores with numLdSt > 32: one thread-block cluster per
                              logical TB, the critical section split over its SMs, for every such run (by
                              default only semaphores whose writers own 4 or more chunks, where it is faster) */

@@ -286,7 +286,6 @@ __device__ __forceinline__ bool cohort_ticket_lock(unsigned* lt, unsigned* lu, u
                       },
                       env, HS_SITE_FA_LOCK);
     pc = cur & 63u;
-    snap = ld_relaxed<GPU>(lt);  // tickets taken so far; its value is needed only at release
     if (ok && pc == 0u) {
       const unsigned g = atom_inc_relaxed<GPU>(gt, wrap);
       unsigned gc = 0;
@@ -301,7 +300,12 @@ __device__ __forceinline__ bool cohort_ticket_lock(unsigned* lt, unsigned* lu, u
                         env, HS_SITE_FA_LOCK);
     }
   }
-  return __syncthreads_or(ok) != 0;
+  const bool got = __syncthreads_or(ok) != 0;
+  // tickets taken so far, read after the CTA barrier so that the barrier does
+  // not wait for it (its value is needed only at release; a ticket taken after
+  // the read only means one global release more)
+  if (is_master()) snap = ld_relaxed<GPU>(lt);
+  return got;
 }
 __device__ __forceinline__ void cohort_ticket_unlock(unsigned* lu, unsigned* gu, unsigned wrap, unsigned my,
                                                      unsigned pc, unsigned snap) {
@@ -335,10 +339,11 @@ __device__ __forceinline__ bool cohort_queue_lock(unsigned* lt, unsigned* lu, Ac
     ok = wait_until_p([&] { cur = ld_acquire<GPU>(lu); return (cur >> 6) == my; }, [&] { return cur; }, [] {}, env,
                       site);
     pc = cur & 63u;
-    snap = ld_relaxed<GPU>(lt);  // tickets taken so far; needed only at release
     if (ok && pc == 0u) ok = acquire();
   }
-  return __syncthreads_or(ok) != 0;
+  const bool got = __syncthreads_or(ok) != 0;
+  if (is_master()) snap = ld_relaxed<GPU>(lt);  // as in cohort_ticket_lock
+  return got;
 }
 template <class Release>
 __device__ __forceinline__ void cohort_queue_unlock(unsigned* lu, Release release, unsigned my, unsigned pc,
@@ -461,7 +466,6 @@ __device__ __forceinline__ bool cohort_sem_writer_wait(unsigned* lt, unsigned* l
     ok = wait_until_p([&] { cur = ld_acquire<GPU>(lu); return (cur >> 6) == my; }, [&] { return cur; }, [] {}, env,
                       HS_SITE_SEM_WAIT);
     pc = cur & 63u;
-    snap = ld_relaxed<GPU>(lt);  // tickets taken so far; needed only at release
     if (ok && pc == 0u) {  // the die's cohort does not hold the semaphore: take it by the writer rule
       ok = wait_until_p(
           [&] {
@@ -473,7 +477,9 @@ __device__ __forceinline__ bool cohort_sem_writer_wait(unsigned* lt, unsigned* l
           [&] { return ld_relaxed<GPU>(st); }, backoff, env, HS_SITE_SEM_WAIT);
     }
   }
-  return __syncthreads_or(ok) != 0;
+  const bool got = __syncthreads_or(ok) != 0;
+  if (is_master()) snap = ld_relaxed<GPU>(lt);  // as in cohort_ticket_lock
+  return got;
 }
 __device__ __forceinline__ void cohort_sem_writer_post(unsigned* lu, unsigned* st, unsigned maxc, unsigned my,
                                                        unsigned pc, unsigned snap) {

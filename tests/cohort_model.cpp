@@ -1,5 +1,5 @@
 // Host model of the cohort (die-aware) protocols of include/hs/hs_device.cuh
-// (cohort_queue_lock / _unlock over a test-and-set word or a ring of slots,
+// (cohort_queue_lock / _unlock over a test-and-set word,
 // cohort_ticket_lock / cohort_ticket_unlock,
 // and the semaphore's cohort writers, cohort_sem_writer_wait / _post, beside
 // readers that follow sem_try_once's reader rule), run by std::threads standing
@@ -10,8 +10,7 @@
 // semaphore, no reader beside a writer and at most N readers at once) and the
 // final state of every lock word.  Test code only.
 //
-//   cohort_model tas|ring|ticket <threads> <iters> <max_pass> <local_wrap> <global_wrap>
-// (for the ring, global_wrap is its last slot index)
+//   cohort_model tas|ticket <threads> <iters> <max_pass> <local_wrap> <global_wrap>
 //   cohort_model sem <threads> <iters> <max_pass> <readers> <N> [local_wrap]
 // prints "ok <counter>" or "FAIL <reason>" and exits 0 / 1.
 #include <atomic>
@@ -49,12 +48,8 @@ void critical_section(int me) {
 }
 
 // --- queue cohort (cohort_queue_lock / _unlock): the die's ticket queue over a
-// global test-and-set word (spin and EBO mutexes) or a global ring of slots
-// (the ring mutex), whose slot travels with the passes through `l_slot`
-u32 kRingMax = 7;
-std::atomic<u32> g_ring[64], g_tail{0}, l_slot[2];
-
-void queue_thread(int me, int die, int iters, bool ring) {
+// global test-and-set word (spin and EBO mutexes)
+void tas_thread(int me, int die, int iters) {
   for (int i = 0; i < iters; ++i) {
     const u32 my = atom_inc(l_ticket[die], kLocalWrap);
     u32 cur;
@@ -62,41 +57,24 @@ void queue_thread(int me, int die, int iters, bool ring) {
     }
     const u32 pc = cur & 63u;
     const u32 snap = l_ticket[die].load(std::memory_order_relaxed);
-    u32 slot = 0;
     if (pc == 0u) {
-      if (ring) {
-        slot = atom_inc(g_tail, kRingMax);
-        while (g_ring[slot].load(std::memory_order_acquire) != 1u) {
-        }
-      } else {
-        for (;;) {
-          u32 z = 0;
-          if (g_word.load(std::memory_order_relaxed) == 0u &&
-              g_word.compare_exchange_weak(z, 1u, std::memory_order_acquire))
-            break;
-        }
+      for (;;) {
+        u32 z = 0;
+        if (g_word.load(std::memory_order_relaxed) == 0u &&
+            g_word.compare_exchange_weak(z, 1u, std::memory_order_acquire))
+          break;
       }
-    } else if (ring) {
-      slot = l_slot[die].load(std::memory_order_relaxed);
     }
     critical_section(me);
-    if (ring) l_slot[die].store(slot, std::memory_order_relaxed);
     const u32 next = (my >= kLocalWrap) ? 0u : my + 1u;
     if (snap != next && pc + 1u < kMaxPass) {
       l_turn[die].store((next << 6) | (pc + 1u), std::memory_order_release);
     } else {
-      if (ring) {
-        g_ring[slot].store(0xFFFFFFFFu, std::memory_order_relaxed);
-        g_ring[slot >= kRingMax ? 0u : slot + 1u].store(1u, std::memory_order_release);
-      } else {
-        g_word.store(0u, std::memory_order_release);
-      }
+      g_word.store(0u, std::memory_order_release);
       l_turn[die].store(next << 6, std::memory_order_release);
     }
   }
 }
-void tas_thread(int me, int die, int iters) { queue_thread(me, die, iters, false); }
-void ring_thread(int me, int die, int iters) { queue_thread(me, die, iters, true); }
 
 // --- ticket cohort: local turn = (ticket << 6) | passes
 void ticket_thread(int me, int die, int iters) {
@@ -182,11 +160,11 @@ void sem_reader_thread(int, int, int iters) {
 
 int main(int argc, char** argv) {
   if (argc != 7 && !(argc == 8 && std::strcmp(argv[1], "sem") == 0)) {
-    std::fprintf(stderr, "usage: cohort_model tas|ring|ticket threads iters max_pass local_wrap global_wrap\n"
+    std::fprintf(stderr, "usage: cohort_model tas|ticket threads iters max_pass local_wrap global_wrap\n"
                          "       cohort_model sem threads iters max_pass readers N\n");
     return 2;
   }
-  const bool tas = std::strcmp(argv[1], "tas") == 0, ring = std::strcmp(argv[1], "ring") == 0;
+  const bool tas = std::strcmp(argv[1], "tas") == 0;
   const int n = std::atoi(argv[2]), iters = std::atoi(argv[3]);
   if (std::strcmp(argv[1], "sem") == 0) {
     kMaxPass = (u32)std::atoi(argv[4]);
@@ -216,28 +194,18 @@ int main(int argc, char** argv) {
   kMaxPass = (u32)std::atoi(argv[4]);
   kLocalWrap = (u32)std::strtoul(argv[5], nullptr, 10);
   kGlobalWrap = (u32)std::strtoul(argv[6], nullptr, 10);
-  if (ring && (kGlobalWrap < 2u || kGlobalWrap >= 64u)) return std::puts("FAIL ring size"), 2;
-  kRingMax = kGlobalWrap;
-  for (u32 k = 0; k < 64; ++k) g_ring[k] = 0;
-  g_ring[0] = 1;  // slot 0 starts with the lock, as the device ring does
   for (int d = 0; d < 2; ++d) {
     l_ticket[d] = 0;
     l_turn[d] = 0;
-    l_slot[d] = 0;
   }
   std::vector<std::thread> ts;
-  for (int t = 0; t < n; ++t) ts.emplace_back(tas ? tas_thread : ring ? ring_thread : ticket_thread, t, t % 2, iters);
+  for (int t = 0; t < n; ++t) ts.emplace_back(tas ? tas_thread : ticket_thread, t, t % 2, iters);
   for (auto& t : ts) t.join();
   const unsigned long long want = (unsigned long long)n * (unsigned long long)iters;
   if (bad.load()) return std::puts("FAIL two holders at once"), 1;
   if (counter != want) return std::printf("FAIL counter %llu of %llu\n", counter, want), 1;
   if (tas && g_word.load() != 0u) return std::puts("FAIL global word held at the end"), 1;
-  if (ring) {  // the slot after the last taken one holds the lock, every other slot is free
-    const u32 head = g_tail.load();
-    for (u32 k = 0; k <= kRingMax; ++k)
-      if ((g_ring[k].load() == 1u) != (k == head)) return std::printf("FAIL ring slot %u at the end\n", k), 1;
-  }
-  if (!tas && !ring && g_ticket.load() != g_turn.load()) return std::puts("FAIL global ticket and turn differ"), 1;
+  if (!tas && g_ticket.load() != g_turn.load()) return std::puts("FAIL global ticket and turn differ"), 1;
   {
     for (int d = 0; d < 2; ++d)
       if ((l_turn[d].load() >> 6) != l_ticket[d].load() || (l_turn[d].load() & 63u) != 0u)

@@ -1,4 +1,5 @@
-"""GPU: the die-aware cohort global mutexes (spin, EBO, ring "sleep", FA).  Final storage
+"""GPU: the die-aware cohort global mutexes (spin, EBO, FA; the ring "sleep"
+mutex stays plain).  Final storage
 must be bit-exact against the golden's closed form with the cohort lock and
 with HS_RUN_NO_COHORT, in every data mode and at every sweep size, including
 repeats that keep the ticket state; the run must report which lock ran."""
@@ -34,6 +35,8 @@ def test_cohort_runs_on_this_part(hs):
     nsm = hs.device_info()["nsm"]
     r = _check(hs, hs.RunConfig("spinMutex", 10, nsm, 20, threads=256, repeats=1, mode="inc"), 1)
     assert r.cohort == 1  # GB300: two dies
+    ring = _check(hs, hs.RunConfig("sleepMutex", 10, nsm, 20, threads=256, repeats=1, mode="inc"), 3)
+    assert ring.cohort == 0  # a queue lock already: no die queue in front of it
     one = _check(hs, hs.RunConfig("spinMutex", 10, 1, 20, threads=256, repeats=1, mode="inc"), 2)
     assert one.cohort == 0  # a single TB needs no lock hand-off
 
@@ -45,10 +48,9 @@ def test_cohort_slice_and_reference_threads(hs, prim):
     _check(hs, hs.RunConfig(prim, 10, 2 * nsm, 30, threads=32, repeats=10, mode="ref"), 4)
 
 
-@pytest.mark.parametrize("prim", ["faMutex", "sleepMutex", "spinMutex"])
+@pytest.mark.parametrize("prim", ["faMutex", "spinMutexEBO", "spinMutex"])
 def test_cohort_ticket_state_kept_across_repeats(hs, prim):
-    # die tickets, turns, the ring and the slot that travels with the passes
-    # carry over from launch to launch
+    # die tickets and turns carry over from launch to launch
     nsm = hs.device_info()["nsm"]
     _check(hs, hs.RunConfig(prim, 10, nsm, 25, threads=256, repeats=1, mode="inc"), 4)  # initialises the state
     cfg = hs.RunConfig(prim, 10, nsm, 25, threads=256, repeats=3, mode="inc", flags=hs.RUN_KEEP_STATE)

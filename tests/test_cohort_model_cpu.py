@@ -1,7 +1,7 @@
 """The cohort (die-aware) protocols, modelled on the host: std::threads stand
 for TBs on two dies and run the device code's encodings (a die ticket queue,
-its turn word carrying the pass count, over a global test-and-set word, a
-global ring of slots whose slot travels with the passes, or a global ticket;
+its turn word carrying the pass count, over a global test-and-set word or a
+global ticket;
 semaphore writers as ticket cohorts over the packed semaphore word, with
 readers beside them).  Small ticket wraps and pass limits drive the
 wrap-around and global release branches.  Mutual exclusion must hold (for the
@@ -39,17 +39,6 @@ def test_cohort_protocol(model, kind, threads, iters, max_pass, lwrap, gwrap):
     if lwrap + 1 < (threads + 1) // 2 + 1:
         pytest.skip("wrap smaller than the waiters of one die")
     p = subprocess.run([model, kind, str(threads), str(iters), str(max_pass), str(lwrap), str(gwrap)],
-                       capture_output=True, text=True, timeout=120)
-    assert p.returncode == 0 and p.stdout.startswith("ok %d" % (threads * iters)), p.stdout + p.stderr
-
-
-@pytest.mark.parametrize("threads,iters,max_pass,lwrap,ring_max", [
-    (4, 20000, 32, (1 << 25) - 1, 8),  # the device's pass limit and ticket wrap
-    (6, 20000, 2, 7, 2),               # three slots: the two dies' heads wrap the ring constantly
-    (5, 20000, 1, 6, 3),               # max_pass 1: every holder takes and frees a slot
-])
-def test_cohort_ring_protocol(model, threads, iters, max_pass, lwrap, ring_max):
-    p = subprocess.run([model, "ring", str(threads), str(iters), str(max_pass), str(lwrap), str(ring_max)],
                        capture_output=True, text=True, timeout=120)
     assert p.returncode == 0 and p.stdout.startswith("ok %d" % (threads * iters)), p.stdout + p.stderr
 
