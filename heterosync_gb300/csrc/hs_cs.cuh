@@ -514,7 +514,10 @@ __device__ __forceinline__ bool cs_chunk_tma_sub(const RunDesc& d, int chunk, Tm
       ok = tma_wait(t, env);
     }
     t.phase ^= 1u;
-    if (!sub_and(bar, T, ok)) return false;
+    if (!sub_and(bar, T, ok)) {
+      if (tid == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");  // earlier tiles' stores
+      return false;
+    }
     unsigned first = 0u;
     if constexpr (MODE == M_INC) {
       const int per_region = d.L * 4, rw4 = (d.L + 1) * 4;
