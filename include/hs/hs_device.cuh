@@ -321,7 +321,7 @@ __device__ __forceinline__ void cohort_ticket_unlock(unsigned* lu, unsigned* gu,
   }
 }
 
-// Ticket cohort over any global lock (the spin, EBO and ring mutexes).  The
+// Ticket cohort over a global lock (the spin and EBO mutexes' test-and-set word).  The
 // local layer is cohort_ticket_lock's (turn = (ticket << 6) | passes, written
 // only by the holder).  A TB whose turn comes without a pass runs `acquire`
 // (master thread; false on timeout) to take the global lock; the releasing
