@@ -260,7 +260,7 @@ __device__ __forceinline__ void ticket_unlock(unsigned* turn, unsigned wrap) {
 // exclusion is the global lock's (held by one cohort) and the local lock's
 // (one holder in the cohort).
 // ---------------------------------------------------------------------------
-constexpr unsigned kCohortMaxPass = 32;
+constexpr unsigned kCohortMaxPass = 63;
 
 // Ticket cohort: a ticket lock per die over the global ticket lock.  The local
 // turn word carries the pass count: turn = (ticket << 6) | passes, written

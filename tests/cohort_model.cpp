@@ -29,7 +29,7 @@ std::atomic<u32> l_ticket[2], l_turn[2];
 std::atomic<int> owner{-1};
 std::atomic<bool> bad{false};
 unsigned long long counter = 0;  // guarded by the lock under test
-u32 kMaxPass = 32, kLocalWrap = (1u << 25) - 1u, kGlobalWrap = 1000000000u;
+u32 kMaxPass = 63, kLocalWrap = (1u << 25) - 1u, kGlobalWrap = 1000000000u;
 
 // atom.inc: old = *p; *p = (old >= lim) ? 0 : old + 1
 u32 atom_inc(std::atomic<u32>& p, u32 lim) {

@@ -29,7 +29,7 @@ def model(tmp_path_factory):
 
 @pytest.mark.parametrize("kind", ["tas", "ticket"])
 @pytest.mark.parametrize("threads,iters,max_pass,lwrap,gwrap", [
-    (4, 20000, 32, (1 << 25) - 1, 1000000000),  # the device's constants
+    (4, 20000, 63, (1 << 25) - 1, 1000000000),  # the device's constants
     (6, 20000, 2, 7, 5),                         # every other op crosses; tickets wrap constantly
     (8, 10000, 32, 3, 1),
     (3, 30000, 1, 6, 2),                         # max_pass 1: never passes, always the global lock
@@ -44,7 +44,7 @@ def test_cohort_protocol(model, kind, threads, iters, max_pass, lwrap, gwrap):
 
 
 @pytest.mark.parametrize("writers,iters,max_pass,readers,n,lwrap", [
-    (4, 20000, 32, 4, 1, (1 << 25) - 1),  # the device's pass limit and ticket wrap, semaphore of 1
+    (4, 20000, 63, 4, 1, (1 << 25) - 1),  # the device's pass limit and ticket wrap, semaphore of 1
     (6, 10000, 2, 3, 2, 7),               # frequent global posts, tickets wrap constantly
     (5, 10000, 1, 6, 10, 5),              # never passes
     (8, 5000, 32, 0, 120, 4),             # writers only (numTBs <= NUM_SM: every TB a writer)
