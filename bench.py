@@ -30,7 +30,8 @@ primitives at one (numTBs, numLdSt) point; steps cycle through the 6 points.
 
 Beside the sweep, outside its timed region, the line carries "fa_mutex_slice"
 (faMutex, 8 TBs, numLdSt 10, 100 iterations: the one-launch slice workload),
-"exchange" (tree barrier with local exchange on thread-block clusters: 592
+"relaxed" (refCounter, splitCounter and seqlocks at 4 x NUM_SM TBs: ops/s and
+the L2-atomic fraction), "exchange" (tree barrier with local exchange on thread-block clusters: 592
 CTAs, fp32[4096] per CTA rotated every episode, 1000 episodes, cluster sizes
 1/2/4/8), "batch" (the 64-instance mixed batch, one launch per instance against
 the autotuned persistent graph-replayed launch), "serve" (the served request
@@ -487,6 +488,55 @@ def exchange_extra(hs):
                                      "the L2 copy rate is a reference point, not its bound"}}
 
 
+def relaxed_extra(hs, nsm):
+    """The relaxed-atomics programs at GB300 sizes (4 x NUM_SM TBs of 256
+    threads), each checked against its known answer: refCounter (every counter
+    back to 0, refCounter.cu:86-98), splitCounter (every counter 1,
+    splitCounter.cu:54-60) and seqlocks (each lock's final sequence number,
+    seqlocks_kernel.cu:193-203).  Best of 3 kernel times; ops as the programs
+    count them; refCounter against the L2 atomic rate (1 atomic per op: 2 adds
+    and 2 decrements per thread and repeat); splitCounter's readers (numTBs
+    relaxed 4-byte loads per reader thread, the reference's atomicAdd(0) reads
+    of splitCounter_kernel.cu:50-61, which it says may be relaxed) against the
+    L2-resident copy rate, its writers (1 red.add each) beside."""
+    atom_peak, same_rate = l2_atomic_peak(hs)
+    G, T = 4 * nsm, 256
+    out = {"workload": "%d TBs x %d threads per program" % (G, T), "l2_atomic_peak": atom_peak,
+           "l2_same_address_rate": same_rate, "programs": {}}
+
+    def best(fn):
+        rs = [fn() for _ in range(3)]
+        return min(rs, key=lambda x: x[-1].elapsed_ms)
+
+    c0, c1, d0, d1, r = best(lambda: hs.refcounter(32, G, T, 64))
+    if c0.any() or c1.any():
+        raise SystemExit("bench: refCounter counters not back to 0")
+    s = r.elapsed_ms * 1e-3
+    out["programs"]["refCounter"] = {"args": "32 sharers, %d TBs, %d threads, 64 repeats" % (G, T),
+                                     "ms": r.elapsed_ms, "ops_per_s": r.ops / s, "atomics_per_s": r.ops / s,
+                                     "l2_atomic_frac": (r.ops / s) / atom_peak if atom_peak else None}
+    c, o, r = best(lambda: hs.splitcounter(G, T))
+    if not np.array_equal(c, np.ones_like(c)):
+        raise SystemExit("bench: splitCounter counters differ from 1")
+    s = r.elapsed_ms * 1e-3
+    thr = G * T
+    read_bytes = (thr // 2) * G * 4
+    l2_gbs = l2_bandwidth_peak(hs)
+    out["programs"]["splitCounter"] = {"args": "%d TBs, %d threads" % (G, T), "ms": r.elapsed_ms,
+                                       "ops_per_s": r.ops / s, "writer_atomics_per_s": (thr // 2) / s,
+                                       "reader_gbs": read_bytes / s * 1e-9,
+                                       "l2_copy_gbs": l2_gbs,
+                                       "l2_frac": (read_bytes / s * 1e-9) / l2_gbs if l2_gbs else None}
+    seq, dd0, dd1, so, r = best(lambda: hs.seqlocks(G, T, 4))
+    for k in range(G // 4):
+        if seq[k] != 2 * 10 * sum(1 for b in range(G) if b % 16 == 0 and b % 4 == k):
+            raise SystemExit("bench: seqlocks sequence number %d differs from its known value" % k)
+    s = r.elapsed_ms * 1e-3
+    out["programs"]["seqlocks"] = {"args": "%d TBs, %d threads, group 4" % (G, T), "ms": r.elapsed_ms,
+                                   "ops_per_s": r.ops / s, "note": "ops: 10 reader or writer rounds per TB"}
+    return out
+
+
 def batch_extra(hs):
     """The 64-instance mixed batch (numTBs log-uniform [4,512], numLdSt [1,128],
     numCSIters [10,5000]): one launch per instance against one persistent
@@ -834,7 +884,8 @@ def main():
                 "note": "the reference's semaphore kernels cannot run on GB300: " + REF_EXCLUDED}
         if not args.no_extras and world == 1:
             for key, fn in (("fa_mutex_slice", lambda h: fa_mutex_slice_extra(h, nsm)), ("exchange", exchange_extra),
-                            ("batch", batch_extra), ("serve", serve_extra), ("uts_geo", uts_geo_extra)):
+                            ("relaxed", lambda h: relaxed_extra(h, nsm)), ("batch", batch_extra),
+                            ("serve", serve_extra), ("uts_geo", uts_geo_extra)):
                 try:
                     out[key] = fn(hs)
                 except SystemExit:
