@@ -88,7 +88,7 @@ REF_CELLS_FILE = os.path.join(tempfile.gettempdir(), "hs_reference_cells.json")
 # one ncu capture (k_mutex, spinMutex, 152 TBs x 256 threads, numLdSt 100): the
 # chunk and the lock word stay L2-resident, so DRAM traffic is the cold first
 # read and does not grow with the launch's operations.
-DRAM_BYTES_PER_LAUNCH = 231168 + 65024
+DRAM_BYTES_PER_LAUNCH = 184320 + 35840
 TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_mutex (spinMutex, 152 TBs x 256, numLdSt 100, "
                   "200 iterations); profiles/k_mutex_spinMutex_152tbs_L100.md")
 
