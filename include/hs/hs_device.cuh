@@ -466,6 +466,9 @@ __device__ __forceinline__ bool cohort_sem_writer_wait(unsigned* lt, unsigned* l
     ok = wait_until_p([&] { cur = ld_acquire<GPU>(lu); return (cur >> 6) == my; }, [&] { return cur; }, [] {}, env,
                       HS_SITE_SEM_WAIT);
     pc = cur & 63u;
+    // tickets taken so far, read before the semaphore wait and the CTA barrier:
+    // measured faster here than after the barrier (the mutexes read it after)
+    snap = ld_relaxed<GPU>(lt);
     if (ok && pc == 0u) {  // the die's cohort does not hold the semaphore: take it by the writer rule
       ok = wait_until_p(
           [&] {
@@ -477,9 +480,7 @@ __device__ __forceinline__ bool cohort_sem_writer_wait(unsigned* lt, unsigned* l
           [&] { return ld_relaxed<GPU>(st); }, backoff, env, HS_SITE_SEM_WAIT);
     }
   }
-  const bool got = __syncthreads_or(ok) != 0;
-  if (is_master()) snap = ld_relaxed<GPU>(lt);  // as in cohort_ticket_lock
-  return got;
+  return __syncthreads_or(ok) != 0;
 }
 __device__ __forceinline__ void cohort_sem_writer_post(unsigned* lu, unsigned* st, unsigned maxc, unsigned my,
                                                        unsigned pc, unsigned snap) {
